@@ -1,0 +1,385 @@
+"""Benchmark of the fused D2Q9 TRT lattice update (MLUPS, HBM roofline).
+
+Workload (one GPU): the large obstacle array -- ny = 2048, nx = 8192
+(16.8 M cells), 400 squares of side 0.02 ny on a seeded jittered 20 x 20
+grid, parabolic Zou-He inlet, Zou-He pressure outlet, no-slip walls, IBB on
+every obstacle link, drag/lift of every obstacle summed every iteration.
+A "step" is one lattice iteration over all cells.  The distributions (2.4 GB
+in FP64) are far larger than the 129 MB L2, so no flush is needed between
+steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision f64]
+    python bench.py --impl reference        # CPU baseline arm (oracle port)
+
+Prints one JSON line.  ``value`` is device-timed whole-job MLUPS with the
+state resident in HBM; ``e2e`` is the same workload driven step by step
+through the host API (BC vectors uploaded from pinned host memory and the
+drag/lift of every obstacle read back every step); ``roofline`` is the bulk
+kernel's algorithmic bytes (9 loads + 9 stores per cell) over its CUDA-event
+time against the measured HBM copy bandwidth; ``cpu_baseline`` is the C
+restatement of the reference kernels (oracle/, OpenMP over all host cores)
+on a bounded sample of the same workload.
+"""
+import argparse
+import contextlib
+import ctypes
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_LU = {"f64": 144, "f32": 72, "f16s": 36, "bf16s": 36}
+FP64_DP_OPS_PER_LU = 67  # DP instructions of the FP64 collision (lbm_device.cuh)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f16s", "bf16s"])
+    ap.add_argument("--ny", type=int, default=2048)
+    ap.add_argument("--forms", default="f32,f16s,bf16s",
+                    help="other storage forms measured in the same run ('' = none)")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(ny):
+    return {"workload": "obstacle_array %dx%d, 400 squares (side 0.02 ny), IBB, Zou-He "
+                        "inlet/outlet, drag+lift every step" % (4 * ny, ny),
+            "nx": 4 * ny, "ny": ny, "n_obstacles": 400,
+            "l2": "state larger than L2 (no flush needed)"}
+
+
+def make_app(ny):
+    from lbm_gb300.apps import obstacle_array
+    app = obstacle_array(L_lbm=ny)
+    app.output_freq = 10 ** 12
+    return app
+
+
+# ---------------------------------------------------------------------------
+# nvidia-smi clock sampler
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        smax = None
+        for p in self.samples:
+            try:
+                sm.append(float(p[0]))
+                smax = float(p[1])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if p[3 + k].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def build_engine(ny, precision, tmp):
+    import lbm_gb300
+    from lbm_gb300.engine import FusedEngine, trace_bc_program
+    app = make_app(ny)
+    with contextlib.redirect_stdout(io.StringIO()):
+        lat = lbm_gb300.lattice(app, precision=precision, output_dir=tmp, verbose=False)
+        lat.generate_image = lambda obstacles: None
+        app.initialize(lat)
+    obstacles, walls, corners = trace_bc_program(app)
+    eng = FusedEngine(lat, obstacles, walls, corners, precision=precision, drag_cap=4096)
+    base, vec, scale = app.bc_schedule(lat)
+    eng.set_bc_schedule(base, vec, scale(np.arange(200000)), it0=0)
+    eng.collide_from_g(0, macro=False)
+    return app, lat, eng
+
+
+def measure_form(ny, precision, steps, warmup, tmp, peak_gbs, dist=None):
+    import torch
+    from lbm_gb300 import _lib
+    app, lat, eng = build_engine(ny, precision, tmp)
+    N = lat.nx * lat.ny
+    stream = torch.cuda.current_stream()
+    it = 1
+    # Warm-up: W steps, then one untimed K-step graph (captures the graph).
+    eng.steps(it, warmup, graph=False)
+    it += warmup
+    eng.steps(it, steps, graph=True)
+    it += steps
+    eng.check_status()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    eng.steps(it, steps, graph=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    it += steps
+    eng.check_status()
+    # Per-kernel times over K more steps (events around each kernel).
+    prof = (ctypes.c_double * 4)()
+    _lib.call("lbm_profile_steps", ctypes.byref(eng.P), it, steps, eng.cur,
+              _lib.FLAG_CHECK_FINITE, prof, ctypes.c_void_p(stream.cuda_stream))
+    eng.cur ^= (steps & 1)
+    it += steps
+    bulk_units = (lat.nx - 2) * (lat.ny - 2)
+    bulk_ms = prof[0]
+    achieved = BYTES_PER_LU[precision] * bulk_units / (bulk_ms * 1e-3) / 1e9
+    res = {
+        "precision": precision,
+        "ms_per_step": ms / steps,
+        "mlups": N * steps / (ms * 1e-3) / 1e6,
+        "kernel_ms": {"bulk": prof[0], "special": prof[1], "drag": prof[2]},
+        "kernels_per_step": int(prof[3]),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": achieved / peak_gbs, "traffic": None,
+                     "bytes_per_unit": BYTES_PER_LU[precision], "units_per_launch": bulk_units},
+        "n_special": eng.n_special, "n_links": eng.n_links,
+    }
+    return res, (app, lat, eng, it)
+
+
+def measure_e2e(app, lat, eng, it, steps):
+    """Step-by-step through the host API: BCs up, one step, drag/lift down."""
+    import torch
+    from lbm_gb300.engine import pack_bc
+    nx, ny = lat.nx, lat.ny
+    base, vec, scale = app.bc_schedule(lat)
+    n_obs = len(eng.obstacles)
+    h_bc = torch.empty(base.size, dtype=torch.float64).pin_memory()
+    h_drag = torch.empty((n_obs, 2), dtype=torch.float64).pin_memory()
+    eng.set_bc_constant(base)
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        m = it + k
+        s = scale([m - 1])[0]
+        h_bc.copy_(torch.from_numpy(base + s * vec))
+        eng.bc_base.copy_(h_bc, non_blocking=True)
+        eng.steps(m, 1, graph=False)
+        slot = (m - 1) % eng.drag_cap
+        h_drag.copy_(eng.drag_hist[slot, :n_obs], non_blocking=True)
+        stream.synchronize()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    return {"value": nx * ny * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS",
+            "h2d_bytes_per_step": int(base.size * 8), "d2h_bytes_per_step": int(n_obs * 2 * 8),
+            "wall_s": wall, "steps": steps}
+
+
+# ---------------------------------------------------------------------------
+# CPU arm (oracle port, all host threads)
+# ---------------------------------------------------------------------------
+def cpu_reference(ny, seconds, min_iters=2):
+    from lbm_gb300 import geometry
+    from oracle import oracle as O
+
+    class _Lat(O.OracleLattice):
+        def add_obstacle(self, obstacle):
+            return geometry.add_obstacle(self, obstacle.polygon, obstacle.tag, self.IBB)
+
+    app = make_app(ny)
+    with tempfile.TemporaryDirectory() as td, contextlib.redirect_stdout(io.StringIO()):
+        lat = _Lat(app, output_dir=os.path.join(td, ""))
+        app.initialize(lat)
+        app.set_inlets(lat, 0)
+        # one untimed iteration, then a bounded sample
+        def iteration(it):
+            app.set_inlets(lat, it)
+            lat.macro()
+            lat.equilibrium()
+            lat.collision_stream()
+            app.set_bc(lat)
+            app.observables(lat, it)
+        iteration(0)
+        t0 = time.perf_counter()
+        n = 0
+        while n < min_iters or time.perf_counter() - t0 < seconds:
+            iteration(1 + n)
+            n += 1
+        dt = time.perf_counter() - t0
+    cells = lat.nx * lat.ny
+    return {"value": cells * n / dt / 1e6, "unit": "MLUPS", "cores": O.threads(),
+            "kind": "port",
+            "sample": "%d iterations of the full %dx%d workload (FP64, C restatement of "
+                      "nb.py with OpenMP cell loops), %.1f s" % (n, lat.nx, lat.ny, dt)}
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    cfg = workload_config(args.ny)
+    cfg["parallelism"] = "replicas%d" % world
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        res = cpu_reference(args.ny, args.cpu_seconds)
+        line = {"metric": "MLUPS", "value": res["value"], "unit": "MLUPS", "impl": "reference",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": cfg,
+                "cpu_baseline": res,
+                "e2e": {"value": res["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local_rank)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = 6789.0
+    peak_src = "fallback"
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath))
+
+    tmp = tempfile.mkdtemp(prefix="lbm_bench_")
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    res, state = measure_form(args.ny, args.precision, args.steps, args.warmup, tmp, peak, dist)
+    clocks = sampler.stop()
+    app, lat, eng, it = state
+    e2e = measure_e2e(app, lat, eng, it, args.e2e_steps)
+    del app, lat, eng, state
+    torch.cuda.empty_cache()
+
+    ms = res["ms_per_step"]
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        e = torch.tensor([e2e["value"]], device="cuda")
+        dist.all_reduce(e, op=dist.ReduceOp.MIN)
+        e2e["value"] = float(e.item()) * world
+    N = 4 * args.ny * args.ny
+    value = N * world / (ms * 1e-3) / 1e6
+
+    forms = {}
+    if rank == 0 and args.forms:
+        for form in [f for f in args.forms.split(",") if f and f != args.precision]:
+            r, st = measure_form(args.ny, form, args.steps, args.warmup, tmp, peak)
+            forms[form] = {"mlups": r["mlups"], "ms_per_step": r["ms_per_step"],
+                           "roofline_frac": r["roofline"]["frac"],
+                           "achieved_gbs": r["roofline"]["achieved"],
+                           "bulk_ms": r["kernel_ms"]["bulk"]}
+            del st
+            torch.cuda.empty_cache()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_reference(args.ny, args.cpu_seconds)
+
+    roof = res["roofline"]
+    if traffic and traffic.get(args.precision):
+        tr = traffic[args.precision]
+        roof["traffic"] = tr.get("bytes_per_launch")
+        roof["traffic_source"] = tr.get("source")
+    roof["peak_source"] = peak_src
+    second = None
+    if args.precision == "f64":
+        rate = FP64_DP_OPS_PER_LU * res["roofline"]["units_per_launch"] / (res["kernel_ms"]["bulk"] * 1e-3)
+        second = {"bound": "fp64_alu", "dp_instr_per_lu": FP64_DP_OPS_PER_LU,
+                  "achieved_ginstr_s": rate / 1e9, "peak_ginstr_s": 602.6,
+                  "peak_source": "DFMA throughput measured on this GB300 model",
+                  "frac": rate / 1e9 / 602.6}
+    line = {
+        "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision, "data": "synthetic", "config": cfg,
+        "roofline": roof, "second_bound": second,
+        "kernel_ms": res["kernel_ms"], "e2e": e2e,
+        "gpu_launches": args.steps * res["kernels_per_step"] + 1,
+        "clocks": clocks, "forms": forms, "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,201 @@
+/*
+ * lbm_gb300 -- C-ABI of the GB300 D2Q9 TRT lattice update.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (cudaStream_t passed as void*; NULL = legacy default stream), returns an
+ * int status (LBM_OK = 0) and never synchronises the device unless stated.
+ * Arrays use the reference layout of jviquerat/lbm: distributions
+ * g[q][i][j] (9 x nx x ny, j fastest), rho[i][j], u[d][i][j], BC vectors
+ * u_left/u_right[d][j], u_top/u_bot[d][i], rho_right[j]
+ * (lbm/src/core/lattice.py:155-174).  Link lists are int32 triples (i, j, q)
+ * in the order produced by lattice.add_obstacle (lattice.py:328-344); negative
+ * i/j wrap like NumPy indices.  On error, lbm_last_error_string() describes
+ * the failure of the calling thread's last call.
+ *
+ * The library owns no caller memory.  Scratch used by the fused engine lives
+ * in buffers the caller passes in lbm_problem (see lbm_problem_scratch_bytes).
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define LBM_OK 0
+#define LBM_ERR_ARG 1          /* bad size, pointer, enum or alignment        */
+#define LBM_ERR_CUDA 2         /* a CUDA runtime call failed                   */
+#define LBM_ERR_NONFINITE 3    /* NaN/Inf detected in the distributions        */
+#define LBM_ERR_UNSUPPORTED 5  /* valid request outside what this build does   */
+
+/* ---- enums ---------------------------------------------------------------- */
+/* Storage/compute forms of the fused engine. */
+#define LBM_PREC_F64 0   /* FP64 storage, FP64 arithmetic (the plain path)          */
+#define LBM_PREC_F32 1   /* FP32 storage of f - w*rho0, FP32 arithmetic              */
+#define LBM_PREC_F16S 2  /* FP16 storage of f - w*rho0, FP32 arithmetic              */
+#define LBM_PREC_BF16S 3 /* BF16 storage of f - w*rho0, FP32 arithmetic              */
+
+/* Wall operations (Zou-He), lbm/src/core/nb.py:121-247. */
+#define LBM_WALL_LEFT_VELOCITY 0
+#define LBM_WALL_RIGHT_VELOCITY 1
+#define LBM_WALL_RIGHT_PRESSURE 2
+#define LBM_WALL_TOP_VELOCITY 3
+#define LBM_WALL_BOTTOM_VELOCITY 4
+
+/* Corners, lbm/src/core/nb.py:250-344. */
+#define LBM_CORNER_BOTTOM_LEFT 0
+#define LBM_CORNER_TOP_LEFT 1
+#define LBM_CORNER_TOP_RIGHT 2
+#define LBM_CORNER_BOTTOM_RIGHT 3
+
+/* Fused-step modes. */
+#define LBM_MODE_COLLIDE_FROM_G 0  /* macro+equilibrium+collide of g (first step)   */
+#define LBM_MODE_STEP 1            /* stream+BC of f_in, then macro+eq+collide      */
+#define LBM_MODE_FINISH 2          /* stream+BC of f_in into g_out, no collision    */
+
+int lbm_abi_version(void);
+const char* lbm_last_error_string(void);
+/* Number of SMs and name of the current device (for logs/tuning). */
+int lbm_device_info(int* sm_count, char* name, int name_len);
+
+/* ---- kernel-level entry points (FP64, one per reference function) ---------- */
+/* lattice.macro, lbm/src/core/lattice.py:178-189. */
+int lbm_macro_f64(const double* g, double* rho, double* u, int nx, int ny, void* stream);
+/* nb_equilibrium, lbm/src/core/nb.py:7-17. */
+int lbm_equilibrium_f64(const double* u, const double* rho, double* g_eq, int nx, int ny,
+                        void* stream);
+/* nb_col_str, lbm/src/core/nb.py:21-45 (collide into g_up, stream into g in place). */
+int lbm_collision_stream_f64(double* g, const double* g_eq, double* g_up, double om_p,
+                             double om_m, int nx, int ny, void* stream);
+/* nb_bounce_back_obstacle, lbm/src/core/nb.py:77-117.  links: n x 3 int32
+ * (i, j, q); p: n IBB distances (ignored when ibb == 0).  Links are applied in
+ * order (the last link that writes a population wins, as in the serial
+ * reference loop). */
+int lbm_bounce_back_f64(int ibb, const int32_t* links, int64_t n, const double* p,
+                        const double* g_up, double* g, int nx, int ny, void* stream);
+/* nb_drag_lift, lbm/src/core/nb.py:49-73.  Writes the raw momentum-exchange
+ * sums out[0] = fx, out[1] = fy (device pointer); the caller normalises
+ * C = -2 F / (R_ref L_ref U_ref^2).  Deterministic (fixed-order FP64 tree).
+ * scratch: device buffer of at least lbm_drag_lift_scratch_bytes(n) bytes. */
+size_t lbm_drag_lift_scratch_bytes(int64_t n);
+int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* g_up, const double* g,
+                      int nx, int ny, double* out, void* scratch, void* stream);
+/* Zou-He walls, lbm/src/core/nb.py:121-247.  wall: LBM_WALL_*; vec is the
+ * wall's (2 x len) velocity vector; rho_right only for RIGHT_PRESSURE. */
+int lbm_zou_he_f64(int wall, double* u, double* rho, double* g, const double* vec,
+                   const double* rho_right, int nx, int ny, void* stream);
+/* Zou-He corners, lbm/src/core/nb.py:250-344.  corner: LBM_CORNER_*. */
+int lbm_zou_he_corner_f64(int corner, double* u, double* rho, double* g, int nx, int ny,
+                          void* stream);
+
+/* ---- fused engine ---------------------------------------------------------- */
+/*
+ * One call advances the lattice by n_steps reference iterations
+ * (lbm/src/core/run.py:24-54: macro, equilibrium, collide-stream, set_bc,
+ * observables) with the state held as post-collision populations (pull
+ * scheme).  Step k of the call reads f[(parity + k) & 1] and writes
+ * f[(parity + k + 1) & 1].
+ *
+ * Special cells = every wall cell plus every fluid cell that owns an obstacle
+ * link; they are re-done by a second kernel that applies, in reference order,
+ * the links (IBB/BB), the wall operations and the corners.  The host supplies
+ * the special-cell table (sorted linear cell indices i*ny + j, CSR offsets
+ * into the link arrays, the special index of each corner's x-neighbour).
+ */
+typedef struct lbm_problem {
+  int32_t nx, ny;
+  int32_t precision;        /* LBM_PREC_*                                        */
+  int32_t ibb;              /* 1: interpolated bounce-back, 0: halfway BB       */
+  double om_p, om_m;        /* TRT relaxation rates (lattice.py:127-131)        */
+  double rho0;              /* storage shift for the shifted forms              */
+
+  /* BC program: wall operations in application order, then corners. */
+  int32_t n_wall_ops;
+  int32_t wall_ops[5];
+  int32_t n_corner_ops;
+  int32_t corner_ops[4];
+  int32_t corner_nb_special[4];  /* special index of each corner's x-neighbour   */
+  int32_t corner_special[4];     /* special index of each corner cell            */
+
+  /* Distributions (storage type per precision), 9 * nx * ny elements each. */
+  void* f[2];
+
+  /* BC vectors at iteration it: value = base + scale[it - scale_it0] * vec.
+   * Packed layout (doubles): u_left[2*ny] | u_right[2*ny] | u_top[2*nx] |
+   * u_bot[2*nx] | rho_right[ny].  vec may be NULL (constant BCs). */
+  const double* bc_base;
+  const double* bc_vec;
+  const double* bc_scale;   /* one scalar per iteration                         */
+  int64_t bc_scale_it0;
+  int64_t bc_scale_len;
+
+  /* Special cells and links. */
+  int32_t n_special;
+  const int32_t* special_cell;        /* [n_special] linear index i*ny + j       */
+  const int32_t* special_link_start;  /* [n_special + 1]                         */
+  int32_t n_links;
+  const int32_t* link_cell;    /* [n_links] linear index of the (wrapped) cell   */
+  const int32_t* link_q;       /* [n_links] link direction (toward the solid)    */
+  const int32_t* link_nb1;     /* [n_links] linear index of x + c_qb (wrapped)   */
+  const int32_t* link_nb2;     /* [n_links] linear index of x + 2 c_qb (wrapped) */
+  const double* link_p;        /* [n_links] IBB distance                         */
+  const int32_t* special_link_ids; /* [sum of CSR] link ids per special cell     */
+  int32_t n_obstacles;
+  const int32_t* obstacle_link_start; /* [n_obstacles + 1] link id ranges        */
+
+  /* Scratch (caller-allocated, lbm_problem_scratch_bytes). */
+  void* scratch;
+  size_t scratch_bytes;
+
+  /* Optional outputs. */
+  double* drag_hist;        /* [drag_cap][n_obstacles][2] raw (fx, fy)          */
+  int64_t drag_cap;         /* ring size in iterations                          */
+  double* rho_out;          /* [nx*ny]   macro rho (see flags)                  */
+  double* u_out;            /* [2*nx*ny] macro u                                */
+  double* g_out;            /* [9*nx*ny] post-BC g (FINISH / COLLIDE_FROM_G in) */
+  uint32_t* status_flags;   /* [1] device word; bit 0 = non-finite detected     */
+} lbm_problem;
+
+/* Flags for lbm_advance. */
+#define LBM_FLAG_MACRO_LAST 1u   /* write rho_out/u_out on the last step's macro */
+#define LBM_FLAG_CHECK_FINITE 2u /* set status bit 0 on NaN/Inf (cheap)          */
+#define LBM_FLAG_WALL_MACRO 4u   /* FINISH: write rho/u written by wall ops      */
+
+size_t lbm_problem_scratch_bytes(const lbm_problem* p);
+/* Advance n_steps iterations.  it0 is the reference iteration number of the
+ * first collision performed by this call (its BCs use iteration it0 - 1 and
+ * its drag output lands in drag_hist[(it0 - 1) % drag_cap]).  parity selects
+ * which of f[0]/f[1] holds the input.  mode: LBM_MODE_*.  For
+ * LBM_MODE_COLLIDE_FROM_G the input is g_out (the post-BC g) and n_steps must
+ * be 1; LBM_MODE_FINISH must have n_steps == 1 and writes g_out. */
+int lbm_advance(const lbm_problem* p, int mode, int64_t it0, int n_steps, int parity,
+                uint32_t flags, void* stream);
+/* Same as lbm_advance(mode = LBM_MODE_STEP) but launched as a cached CUDA
+ * graph of n_steps iterations (captured on first use per (problem, n_steps,
+ * parity); a graph is re-captured when the problem descriptor changes). */
+int lbm_advance_graph(const lbm_problem* p, int64_t it0, int n_steps, int parity,
+                      uint32_t flags, void* stream);
+/* Per-kernel timing: runs n_steps LBM_MODE_STEP iterations (no graph) with
+ * CUDA events around each kernel and synchronises.  ms_out[0..2] = average
+ * milliseconds of the bulk, special-cell and drag kernels per step,
+ * ms_out[3] = kernels launched per step. */
+int lbm_profile_steps(const lbm_problem* p, int64_t it0, int n_steps, int parity, uint32_t flags,
+                      double* ms_out, void* stream);
+/* Drop every cached graph (call before freeing buffers a graph refers to). */
+int lbm_graph_cache_clear(void);
+
+/* Convert distributions between the FP64 reference layout and a storage form
+ * (shifted forms store f - w_q * rho0).  n_cells = nx * ny. */
+int lbm_pack_f64(int precision, const double* g, void* f, int64_t n_cells, double rho0,
+                 void* stream);
+int lbm_unpack_f64(int precision, const void* f, double* g, int64_t n_cells, double rho0,
+                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

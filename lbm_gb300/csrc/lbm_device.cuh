@@ -1,0 +1,290 @@
+// Device-side building blocks of the D2Q9 TRT lattice update.
+//
+// D2Q9 order c = (0,0),(1,0),(-1,0),(0,1),(0,-1),(1,1),(-1,-1),(-1,1),(1,-1),
+// opposite ns = 0,2,1,4,3,6,5,8,7 and weights 4/9, 1/9 x4, 1/36 x4, as in the
+// reference (lbm/src/core/lattice.py:135-152).  Distributions are stored
+// q-major, g[q][i][j] with j fastest (lattice.py:155-157): plane q of a
+// lattice with N = nx*ny cells starts at q*N and cell (i, j) is i*ny + j.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace lbm {
+
+__host__ __device__ constexpr int cx(int q) {
+  return q == 1 || q == 5 || q == 8 ? 1 : (q == 2 || q == 6 || q == 7 ? -1 : 0);
+}
+__host__ __device__ constexpr int cy(int q) {
+  return q == 3 || q == 5 || q == 7 ? 1 : (q == 4 || q == 6 || q == 8 ? -1 : 0);
+}
+__host__ __device__ constexpr int opp(int q) {
+  return q == 0 ? 0 : (q & 1 ? q + 1 : q - 1);
+}
+__host__ __device__ constexpr double wgt(int q) {
+  return q == 0 ? 4.0 / 9.0 : (q < 5 ? 1.0 / 9.0 : 1.0 / 36.0);
+}
+
+// ---------------------------------------------------------------------------
+// Reciprocal.  FP64: hardware approximation (PTX rcp.approx.ftz.f64) refined
+// by one third-order Householder step r <- r + r*(e + e^2), e = 1 - x*r
+// (Householder, "The Numerical Treatment of a Single Nonlinear Equation",
+// 1970); the error after the step is about 1 ulp for the density range of a
+// lattice (|rho - 1| << 1).  FP32: plain IEEE division by the compiler.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double recip(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  double e2 = fma(e, e, e);
+  return fma(r, e2, r);
+}
+__device__ __forceinline__ float recip(float x) { return 1.0f / x; }
+
+// ---------------------------------------------------------------------------
+// Storage forms.  Full-precision values are T (double for F64, float for the
+// reduced forms); shifted forms store d = f - w_q * rho0.
+// ---------------------------------------------------------------------------
+struct StoreF64 {
+  using S = double;
+  using T = double;
+  static constexpr bool kShift = false;
+  __device__ static T load(const S* p) { return *p; }
+  __device__ static void store(S* p, T v) { *p = v; }
+};
+struct StoreF32 {
+  using S = float;
+  using T = float;
+  static constexpr bool kShift = true;
+  __device__ static T load(const S* p) { return *p; }
+  __device__ static void store(S* p, T v) { *p = v; }
+};
+struct StoreF16 {
+  using S = __half;
+  using T = float;
+  static constexpr bool kShift = true;
+  __device__ static T load(const S* p) { return __half2float(*p); }
+  __device__ static void store(S* p, T v) { *p = __float2half_rn(v); }
+};
+struct StoreBF16 {
+  using S = __nv_bfloat16;
+  using T = float;
+  static constexpr bool kShift = true;
+  __device__ static T load(const S* p) { return __bfloat162float(*p); }
+  __device__ static void store(S* p, T v) { *p = __float2bfloat16_rn(v); }
+};
+
+// ---------------------------------------------------------------------------
+// TRT collision coefficients (lattice.py:127-131; nb.py:32-35 rewritten in the
+// symmetric/antisymmetric pair form).  With a = 1 - (om_p + om_m)/2 and
+// b = (om_p - om_m)/2 the reference update
+//   g_up_q = a g_q - b g_qb + (a' g_eq_q + b g_eq_qb),  a' = (om_p + om_m)/2
+// equals, for the pair (q, qb) with t = 3 c_q.u,
+//   g_up_q  = a d_q  - b d_qb + w om_p (drho + rho(t^2/2 - v)) + w om_m rho t
+//   g_up_qb = a d_qb - b d_q  + w om_p (drho + rho(t^2/2 - v)) - w om_m rho t
+// where d = g - w rho0 and drho = rho - rho0 (rho0 = 0 for the plain form).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Coef {
+  T a, mb;          // a, -b
+  T a0, p0;         // q = 0: 1 - om_p, om_p * w0
+  T wp1, wm1;       // om_p * w1, 3 * om_m * w1  (axis pairs)
+  T wp2, wm2;       // om_p * w2, 3 * om_m * w2  (diagonal pairs)
+  T rho0;
+  T w[9];           // weights * rho0 (shift of each population)
+};
+
+template <typename T>
+__host__ __device__ inline Coef<T> make_coef(double om_p, double om_m, double rho0) {
+  Coef<T> k;
+  double a = 1.0 - 0.5 * (om_p + om_m);
+  double b = 0.5 * (om_p - om_m);
+  k.a = (T)a;
+  k.mb = (T)(-b);
+  k.a0 = (T)(1.0 - om_p);
+  k.p0 = (T)(om_p * (4.0 / 9.0));
+  k.wp1 = (T)(om_p * (1.0 / 9.0));
+  k.wm1 = (T)(3.0 * om_m * (1.0 / 9.0));
+  k.wp2 = (T)(om_p * (1.0 / 36.0));
+  k.wm2 = (T)(3.0 * om_m * (1.0 / 36.0));
+  k.rho0 = (T)rho0;
+  for (int q = 0; q < 9; ++q) k.w[q] = (T)(wgt(q) * rho0);
+  return k;
+}
+
+// Moments of the (shifted) populations d[0..8]: drho = sum d, j = sum c d,
+// rho = rho0 + drho, u = j / rho.
+template <typename T, bool SHIFT>
+struct Moments {
+  T drho, rho, jx, jy, ux, uy;
+};
+
+template <typename T, bool SHIFT>
+__device__ __forceinline__ Moments<T, SHIFT> moments(const T d[9], T rho0) {
+  Moments<T, SHIFT> m;
+  T s12 = d[1] + d[2], s34 = d[3] + d[4], s56 = d[5] + d[6], s78 = d[7] + d[8];
+  T d12 = d[1] - d[2], d34 = d[3] - d[4], d56 = d[5] - d[6], d87 = d[8] - d[7];
+  m.drho = (((d[0] + s12) + s34) + s56) + s78;
+  m.rho = SHIFT ? rho0 + m.drho : m.drho;
+  m.jx = (d12 + d56) + d87;
+  m.jy = (d34 + d56) - d87;
+  T r = recip(m.rho);
+  m.ux = m.jx * r;
+  m.uy = m.jy * r;
+  return m;
+}
+
+// In-place TRT collision of d[0..8] given its moments.
+template <typename T, bool SHIFT>
+__device__ __forceinline__ void collide(T d[9], const Moments<T, SHIFT>& m, const Coef<T>& k) {
+  const T jx = m.jx, jy = m.jy, ux = m.ux, uy = m.uy;
+  const T Qx = jx * ux, Qy = jy * uy;
+  const T j5 = jx + jy, u5 = ux + uy, Q5 = j5 * u5;
+  const T j7 = jy - jx, u7 = uy - ux, Q7 = j7 * u7;
+  // R = drho - rho*v  with rho*v = 1.5 (jx ux + jy uy)
+  const T R = fma(T(-1.5), Qx + Qy, m.drho);
+  d[0] = fma(k.a0, d[0], k.p0 * R);
+#define LBM_PAIR(q, qb, Q, cj, wp, wm)             \
+  {                                                \
+    const T P = fma(T(4.5), Q, R);                 \
+    const T M = (wm) * (cj);                       \
+    const T base = (wp) * P;                       \
+    const T dq = d[q], dqb = d[qb];                \
+    d[q] = fma(k.a, dq, fma(k.mb, dqb, base + M)); \
+    d[qb] = fma(k.a, dqb, fma(k.mb, dq, base - M)); \
+  }
+  LBM_PAIR(1, 2, Qx, jx, k.wp1, k.wm1)
+  LBM_PAIR(3, 4, Qy, jy, k.wp1, k.wm1)
+  LBM_PAIR(5, 6, Q5, j5, k.wp2, k.wm2)
+  LBM_PAIR(7, 8, Q7, j7, k.wp2, k.wm2)
+#undef LBM_PAIR
+}
+
+// ---------------------------------------------------------------------------
+// Boundary operations on full (unshifted) populations of one cell, written in
+// the operation order of the reference expressions.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct CellBC {
+  T g[9];
+  T rho, ux, uy;
+};
+
+// nb_zou_he_left_wall_velocity, nb.py:121-143.
+template <typename T>
+__device__ __forceinline__ void zh_left(CellBC<T>& c, T ubx, T uby) {
+  const T C1 = T(2.0 / 3.0), C2 = T(1.0 / 6.0), C3 = T(0.5);
+  c.ux = ubx;
+  c.uy = uby;
+  T r = (c.g[0] + c.g[3] + c.g[4] + T(2) * c.g[2] + T(2) * c.g[6] + T(2) * c.g[7]) / (T(1) - c.ux);
+  c.rho = r;
+  c.g[1] = c.g[2] + C1 * r * c.ux;
+  c.g[5] = c.g[6] - C3 * (c.g[3] - c.g[4]) + C2 * r * c.ux + C3 * r * c.uy;
+  c.g[8] = c.g[7] + C3 * (c.g[3] - c.g[4]) + C2 * r * c.ux - C3 * r * c.uy;
+}
+// nb_zou_he_right_wall_velocity, nb.py:147-169.
+template <typename T>
+__device__ __forceinline__ void zh_right(CellBC<T>& c, T ubx, T uby) {
+  const T C1 = T(2.0 / 3.0), C2 = T(1.0 / 6.0), C3 = T(0.5);
+  c.ux = ubx;
+  c.uy = uby;
+  T r = (c.g[0] + c.g[3] + c.g[4] + T(2) * c.g[1] + T(2) * c.g[5] + T(2) * c.g[8]) / (T(1) + c.ux);
+  c.rho = r;
+  c.g[2] = c.g[1] - C1 * r * c.ux;
+  c.g[6] = c.g[5] + C3 * (c.g[3] - c.g[4]) - C2 * r * c.ux - C3 * r * c.uy;
+  c.g[7] = c.g[8] - C3 * (c.g[3] - c.g[4]) - C2 * r * c.ux + C3 * r * c.uy;
+}
+// nb_zou_he_right_wall_pressure, nb.py:173-195.
+template <typename T>
+__device__ __forceinline__ void zh_right_pressure(CellBC<T>& c, T rho_b, T uby) {
+  const T C1 = T(2.0 / 3.0), C2 = T(1.0 / 6.0), C3 = T(0.5);
+  c.rho = rho_b;
+  c.uy = uby;
+  T r = c.rho;
+  c.ux = (c.g[0] + c.g[3] + c.g[4] + T(2) * c.g[1] + T(2) * c.g[5] + T(2) * c.g[8]) / r - T(1);
+  c.g[2] = c.g[1] - C1 * r * c.ux;
+  c.g[6] = c.g[5] + C3 * (c.g[3] - c.g[4]) - C2 * r * c.ux - C3 * r * c.uy;
+  c.g[7] = c.g[8] - C3 * (c.g[3] - c.g[4]) - C2 * r * c.ux + C3 * r * c.uy;
+}
+// nb_zou_he_top_wall_velocity, nb.py:199-221.
+template <typename T>
+__device__ __forceinline__ void zh_top(CellBC<T>& c, T ubx, T uby) {
+  const T C1 = T(2.0 / 3.0), C2 = T(1.0 / 6.0), C3 = T(0.5);
+  c.ux = ubx;
+  c.uy = uby;
+  T r = (c.g[0] + c.g[1] + c.g[2] + T(2) * c.g[3] + T(2) * c.g[5] + T(2) * c.g[7]) / (T(1) + c.uy);
+  c.rho = r;
+  c.g[4] = c.g[3] - C1 * r * c.uy;
+  c.g[8] = c.g[7] - C3 * (c.g[1] - c.g[2]) + C3 * r * c.ux - C2 * r * c.uy;
+  c.g[6] = c.g[5] + C3 * (c.g[1] - c.g[2]) - C3 * r * c.ux - C2 * r * c.uy;
+}
+// nb_zou_he_bottom_wall_velocity, nb.py:225-247.
+template <typename T>
+__device__ __forceinline__ void zh_bottom(CellBC<T>& c, T ubx, T uby) {
+  const T C1 = T(2.0 / 3.0), C2 = T(1.0 / 6.0), C3 = T(0.5);
+  c.ux = ubx;
+  c.uy = uby;
+  T r = (c.g[0] + c.g[1] + c.g[2] + T(2) * c.g[4] + T(2) * c.g[6] + T(2) * c.g[8]) / (T(1) - c.uy);
+  c.rho = r;
+  c.g[3] = c.g[4] + C1 * r * c.uy;
+  c.g[5] = c.g[6] - C3 * (c.g[1] - c.g[2]) + C3 * r * c.ux + C2 * r * c.uy;
+  c.g[7] = c.g[8] + C3 * (c.g[1] - c.g[2]) - C3 * r * c.ux + C2 * r * c.uy;
+}
+
+// Corners, nb.py:250-344.  rho/u are first copied from the x-neighbour.
+template <typename T>
+__device__ __forceinline__ void zh_corner(int corner, CellBC<T>& c, T rho_nb, T ux_nb, T uy_nb) {
+  const T C23 = T(2.0 / 3.0), C16 = T(1.0 / 6.0);
+  c.ux = ux_nb;
+  c.uy = uy_nb;
+  c.rho = rho_nb;
+  const T r = c.rho, ux = c.ux, uy = c.uy;
+  switch (corner) {
+    case 0:  // bottom-left, nb.py:251-271
+      c.g[1] = c.g[2] + C23 * r * ux;
+      c.g[3] = c.g[4] + C23 * r * uy;
+      c.g[5] = c.g[6] + C16 * r * ux + C16 * r * uy;
+      c.g[7] = T(0);
+      c.g[8] = T(0);
+      break;
+    case 1:  // top-left, nb.py:275-296
+      c.g[1] = c.g[2] + C23 * r * ux;
+      c.g[4] = c.g[3] - C23 * r * uy;
+      c.g[8] = c.g[7] + C16 * r * ux - C16 * r * uy;
+      c.g[5] = T(0);
+      c.g[6] = T(0);
+      break;
+    case 2:  // top-right, nb.py:300-320
+      c.g[2] = c.g[1] - C23 * r * ux;
+      c.g[4] = c.g[3] - C23 * r * uy;
+      c.g[6] = c.g[5] - C16 * r * ux - C16 * r * uy;
+      c.g[7] = T(0);
+      c.g[8] = T(0);
+      break;
+    default:  // bottom-right, nb.py:324-344
+      c.g[2] = c.g[1] - C23 * r * ux;
+      c.g[3] = c.g[4] + C23 * r * uy;
+      c.g[7] = c.g[8] - C16 * r * ux + C16 * r * uy;
+      c.g[5] = T(0);
+      c.g[6] = T(0);
+      break;
+  }
+  c.g[0] = r - c.g[1] - c.g[2] - c.g[3] - c.g[4] - c.g[5] - c.g[6] - c.g[7] - c.g[8];
+}
+
+// Interpolated / halfway bounce-back of one link, nb.py:77-117.
+// up_q_x = g_up[q, x], up_q_1 = g_up[q, x + c_qb], up_q_2 = g_up[q, x + 2 c_qb],
+// up_qb_x = g_up[qb, x], up_qb_1 = g_up[qb, x + c_qb].
+template <typename T>
+__device__ __forceinline__ T ibb_value(T p, T up_q_x, T up_q_1, T up_q_2, T up_qb_x, T up_qb_1) {
+  const T pp = T(2) * p;
+  if (p < T(0.5)) {
+    return p * (pp + T(1)) * up_q_x + (T(1) + pp) * (T(1) - pp) * up_q_1 -
+           p * (T(1) - pp) * up_q_2;
+  }
+  return (T(1) / (p * (pp + T(1)))) * up_q_x + ((pp - T(1)) / p) * up_qb_x +
+         ((T(1) - pp) / (T(1) + pp)) * up_qb_1;
+}
+
+}  // namespace lbm

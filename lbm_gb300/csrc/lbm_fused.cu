@@ -1,0 +1,502 @@
+// Fused D2Q9 TRT lattice update (pull scheme), all storage forms.
+//
+// One reference iteration (lbm/src/core/run.py:24-54) is split at the
+// collision: the state kept in HBM is the post-collision population g_up of
+// the previous iteration.  Iteration `it` then reads g_up(it-1), streams it
+// (pull), applies set_bc(it-1) and the drag/lift of it-1, and takes macro,
+// equilibrium and collision of g(it) to write g_up(it).  Two kernels do this:
+//
+//   k_bulk    every cell not on a wall: pull 9 values, collide, write 9.
+//   k_special every wall cell and every cell owning an obstacle link (a short
+//             sorted list): pull, links (IBB/BB), Zou-He walls in the app's
+//             order, corners, per-link drag terms, collide.  It overwrites
+//             what k_bulk wrote at link cells.
+//   k_drag    per obstacle, a fixed-order FP64 tree over the per-link terms.
+//
+// Edge populations without an in-domain source keep the previous post-BC
+// value (nb.py:38-45 streams interior slices only); k_special keeps those
+// values, and the previous macro rho/u of every special cell that corners
+// read (nb.py:254-257), in ping-pong scratch buffers.
+#include "lbm_device.cuh"
+#include "lbm_internal.h"
+
+#include <string.h>
+
+namespace lbm {
+
+struct FusedArgs {
+  int nx, ny;
+  long long N;          // nx * ny
+  Coef<double> kd;
+  Coef<float> kf;
+  const void* fin;
+  void* fout;
+  // BC program
+  int n_wall_ops;
+  int wall_ops[5];
+  int n_corner_ops;
+  int corner_ops[4];
+  int corner_nb_special[4];
+  int corner_special[4];
+  int ibb;
+  // BC vectors: value(it) = base + scale[it - scale_it0] * vec
+  const double* bc_base;
+  const double* bc_vec;
+  const double* bc_scale;
+  long long bc_scale_it0, bc_scale_len;
+  // Device iteration counter: the iteration whose collision the running step
+  // does.  k_bulk (first kernel of a step) advances it, so a captured graph
+  // replays correctly from any starting iteration.
+  long long* it_dev;
+  int advance_it;
+  // special cells / links
+  int n_special;
+  const int* special_cell;
+  const int* special_link_start;
+  const int* special_link_ids;
+  const int* link_cell;
+  const int* link_q;
+  const int* link_nb1;
+  const int* link_nb2;
+  const double* link_p;
+  // scratch: halves alternate with the parity of the iteration number
+  double* stale[2];         // [9][n_special] post-BC g of an iteration
+  double* mac[2];           // [3][n_special] macro rho, ux, uy of an iteration
+  double* link_force;       // [2][n_links]
+  int n_links;
+  // drag/lift history
+  double* drag_hist;
+  long long drag_cap;
+  int n_obs;
+  const int* obs_start;
+  // outputs
+  double* rho_out;
+  double* u_out;
+  double* g_out;
+  unsigned* status;
+  int mode;
+  int write_macro;
+  int wall_macro;
+  int check_finite;
+};
+
+template <typename T>
+__device__ __forceinline__ const Coef<T>& coef(const FusedArgs& a);
+template <>
+__device__ __forceinline__ const Coef<double>& coef<double>(const FusedArgs& a) { return a.kd; }
+template <>
+__device__ __forceinline__ const Coef<float>& coef<float>(const FusedArgs& a) { return a.kf; }
+
+// Scale of the BC vectors at iteration bc_it (status bit 1 if not covered).
+__device__ __forceinline__ double bc_scale_at(const FusedArgs& a, long long bc_it) {
+  if (!a.bc_vec) return 0.0;
+  long long idx = bc_it - a.bc_scale_it0;
+  if (idx < 0 || idx >= a.bc_scale_len) {
+    if (a.status) atomicOr(a.status, 2u);
+    return 0.0;
+  }
+  return a.bc_scale[idx];
+}
+
+__device__ __forceinline__ double bc_value(const FusedArgs& a, double s, int off) {
+  double b = a.bc_base[off];
+  return a.bc_vec ? fma(s, a.bc_vec[off], b) : b;
+}
+
+// ---------------------------------------------------------------------------
+// Bulk kernel: every non-wall cell.
+// ---------------------------------------------------------------------------
+template <class St, int MODE>
+__global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
+  using S = typename St::S;
+  using T = typename St::T;
+  const long long N = a.N;
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell == 0 && a.advance_it) *a.it_dev += 1;
+  if (cell >= N) return;
+  const int i = (int)(cell / a.ny);
+  const int j = (int)(cell - (long long)i * a.ny);
+  const S* fin = (const S*)a.fin;
+  const Coef<T>& k = coef<T>(a);
+  T d[9];
+  if (MODE == LBM_MODE_COLLIDE_FROM_G) {
+    // Input is the full post-BC g (FP64) of every cell, edges included.
+#pragma unroll
+    for (int q = 0; q < 9; ++q) d[q] = (T)a.g_out[q * N + cell] - (St::kShift ? k.w[q] : T(0));
+  } else {
+    if (i == 0 || i == a.nx - 1 || j == 0 || j == a.ny - 1) return;
+    const long long ny = a.ny;
+    d[0] = St::load(fin + cell);
+    d[1] = St::load(fin + 1 * N + cell - ny);
+    d[2] = St::load(fin + 2 * N + cell + ny);
+    d[3] = St::load(fin + 3 * N + cell - 1);
+    d[4] = St::load(fin + 4 * N + cell + 1);
+    d[5] = St::load(fin + 5 * N + cell - ny - 1);
+    d[6] = St::load(fin + 6 * N + cell + ny + 1);
+    d[7] = St::load(fin + 7 * N + cell + ny - 1);
+    d[8] = St::load(fin + 8 * N + cell - ny + 1);
+    if (MODE == LBM_MODE_FINISH) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) a.g_out[q * N + cell] = (double)(d[q] + (St::kShift ? k.w[q] : T(0)));
+      return;
+    }
+  }
+  Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+  if (a.write_macro) {
+    a.rho_out[cell] = (double)m.rho;
+    a.u_out[cell] = (double)m.ux;
+    a.u_out[N + cell] = (double)m.uy;
+  }
+  if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
+  collide<T, St::kShift>(d, m, k);
+  S* fout = (S*)a.fout;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) St::store(fout + q * N + cell, d[q]);
+}
+
+// ---------------------------------------------------------------------------
+// Special cells.
+// ---------------------------------------------------------------------------
+// Post-BC state of special cell s without corners (pull, links, wall ops).
+template <class St>
+__device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<double>& c) {
+  using S = typename St::S;
+  using T = typename St::T;
+  const long long N = a.N;
+  const int ny = a.ny, nx = a.nx;
+  const int cell = a.special_cell[s];
+  const int i = cell / ny, j = cell - i * ny;
+  const S* fin = (const S*)a.fin;
+  const double rho0 = St::kShift ? (double)a.kd.rho0 : 0.0;
+  const double* stale_in = a.stale[(it - 1) & 1];
+  const double* mac_in = a.mac[(it - 1) & 1];
+  const double bs = bc_scale_at(a, it - 1);
+  // Pull (or keep the stale post-BC value where the source is outside).
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const int si = i - cx(q), sj = j - cy(q);
+    if (si >= 0 && si < nx && sj >= 0 && sj < ny) {
+      c.g[q] = (double)St::load(fin + q * N + (long long)si * ny + sj) + wgt(q) * rho0;
+    } else {
+      c.g[q] = stale_in[(long long)q * a.n_special + s];
+    }
+  }
+  c.rho = mac_in[s];
+  c.ux = mac_in[a.n_special + s];
+  c.uy = mac_in[2 * a.n_special + s];
+  // Obstacle links, in reference order (nb.py:77-117).
+  const int l0 = a.special_link_start[s], l1 = a.special_link_start[s + 1];
+  for (int l = l0; l < l1; ++l) {
+    const int k = a.special_link_ids[l];
+    const int q = a.link_q[k], qb = opp(q);
+    const long long x = a.link_cell[k];
+    const double up_q_x = (double)St::load(fin + q * N + x) + wgt(q) * rho0;
+    if (a.ibb) {
+      const double p = a.link_p[k];
+      const long long x1 = a.link_nb1[k];
+      if (p < 0.5) {
+        const long long x2 = a.link_nb2[k];
+        const double up_q_1 = (double)St::load(fin + q * N + x1) + wgt(q) * rho0;
+        const double up_q_2 = (double)St::load(fin + q * N + x2) + wgt(q) * rho0;
+        c.g[qb] = ibb_value<double>(p, up_q_x, up_q_1, up_q_2, 0.0, 0.0);
+      } else {
+        const double up_qb_x = (double)St::load(fin + qb * N + x) + wgt(qb) * rho0;
+        const double up_qb_1 = (double)St::load(fin + qb * N + x1) + wgt(qb) * rho0;
+        c.g[qb] = ibb_value<double>(p, up_q_x, 0.0, 0.0, up_qb_x, up_qb_1);
+      }
+    } else {
+      c.g[qb] = up_q_x;
+    }
+  }
+  // Zou-He walls in the app's order (nb.py:121-247).
+  const int off_ur = 2 * ny, off_ut = 4 * ny, off_ub = 4 * ny + 2 * nx, off_rr = 4 * ny + 4 * nx;
+  for (int w = 0; w < a.n_wall_ops; ++w) {
+    switch (a.wall_ops[w]) {
+      case LBM_WALL_LEFT_VELOCITY:
+        if (i == 0) zh_left<double>(c, bc_value(a, bs, j), bc_value(a, bs, ny + j));
+        break;
+      case LBM_WALL_RIGHT_VELOCITY:
+        if (i == nx - 1) zh_right<double>(c, bc_value(a, bs, off_ur + j), bc_value(a, bs, off_ur + ny + j));
+        break;
+      case LBM_WALL_RIGHT_PRESSURE:
+        if (i == nx - 1) zh_right_pressure<double>(c, bc_value(a, bs, off_rr + j), bc_value(a, bs, off_ur + ny + j));
+        break;
+      case LBM_WALL_TOP_VELOCITY:
+        if (j == ny - 1) zh_top<double>(c, bc_value(a, bs, off_ut + i), bc_value(a, bs, off_ut + nx + i));
+        break;
+      case LBM_WALL_BOTTOM_VELOCITY:
+        if (j == 0) zh_bottom<double>(c, bc_value(a, bs, off_ub + i), bc_value(a, bs, off_ub + nx + i));
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+__device__ __forceinline__ bool on_wall_op(const FusedArgs& a, int i, int j) {
+  for (int w = 0; w < a.n_wall_ops; ++w) {
+    const int op = a.wall_ops[w];
+    if (op == LBM_WALL_LEFT_VELOCITY && i == 0) return true;
+    if ((op == LBM_WALL_RIGHT_VELOCITY || op == LBM_WALL_RIGHT_PRESSURE) && i == a.nx - 1) return true;
+    if (op == LBM_WALL_TOP_VELOCITY && j == a.ny - 1) return true;
+    if (op == LBM_WALL_BOTTOM_VELOCITY && j == 0) return true;
+  }
+  return false;
+}
+
+template <class St, int MODE>
+__global__ void __launch_bounds__(128) k_special(FusedArgs a) {
+  using S = typename St::S;
+  using T = typename St::T;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n_special) return;
+  const long long N = a.N;
+  const int ny = a.ny;
+  const int cell = a.special_cell[s];
+  const int i = cell / ny, j = cell - i * ny;
+  const Coef<T>& k = coef<T>(a);
+  const double rho0 = St::kShift ? (double)a.kd.rho0 : 0.0;
+  const long long it = *a.it_dev;
+  CellBC<double> c;
+  if (MODE == LBM_MODE_COLLIDE_FROM_G) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) c.g[q] = a.g_out[q * N + cell];
+  } else {
+    bc_chain<St>(a, it, s, c);
+    // Corners (nb.py:250-344): rho/u of the x-neighbour after its wall ops.
+    for (int w = 0; w < a.n_corner_ops; ++w) {
+      const int cn = a.corner_ops[w];
+      if (a.corner_special[cn] != s) continue;
+      CellBC<double> nb;
+      bc_chain<St>(a, it, a.corner_nb_special[cn], nb);
+      zh_corner<double>(cn, c, nb.rho, nb.ux, nb.uy);
+    }
+    // Per-link momentum exchange terms (nb.py:49-73) with the post-BC g.
+    const int l0 = a.special_link_start[s], l1 = a.special_link_start[s + 1];
+    const S* fin = (const S*)a.fin;
+    for (int l = l0; l < l1; ++l) {
+      const int kk = a.special_link_ids[l];
+      const int q = a.link_q[kk];
+      const double g0 = ((double)St::load(fin + q * N + cell) + wgt(q) * rho0) + c.g[opp(q)];
+      a.link_force[kk] = g0 * (double)cx(q);
+      a.link_force[a.n_links + kk] = g0 * (double)cy(q);
+    }
+    if (MODE == LBM_MODE_FINISH) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) a.g_out[q * N + cell] = c.g[q];
+      if (a.wall_macro && on_wall_op(a, i, j)) {
+        a.rho_out[cell] = c.rho;
+        a.u_out[cell] = c.ux;
+        a.u_out[N + cell] = c.uy;
+      }
+      bool corner_cell = false;
+      for (int w = 0; w < a.n_corner_ops; ++w) corner_cell |= (a.corner_special[a.corner_ops[w]] == s);
+      if (a.wall_macro && corner_cell) {
+        a.rho_out[cell] = c.rho;
+        a.u_out[cell] = c.ux;
+        a.u_out[N + cell] = c.uy;
+      }
+      return;
+    }
+  }
+  // Keep the post-BC value for the next iteration's edge pulls.
+  double* stale_out = a.stale[it & 1];
+  double* mac_out = a.mac[it & 1];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) stale_out[(long long)q * a.n_special + s] = c.g[q];
+  // Macro + collision in the storage form's arithmetic.
+  T d[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) d[q] = (T)(c.g[q] - wgt(q) * rho0);
+  Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+  mac_out[s] = (double)m.rho;
+  mac_out[a.n_special + s] = (double)m.ux;
+  mac_out[2 * a.n_special + s] = (double)m.uy;
+  if (a.write_macro) {
+    a.rho_out[cell] = (double)m.rho;
+    a.u_out[cell] = (double)m.ux;
+    a.u_out[N + cell] = (double)m.uy;
+  }
+  if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
+  collide<T, St::kShift>(d, m, k);
+  S* fout = (S*)a.fout;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) St::store(fout + q * N + cell, d[q]);
+}
+
+// Per-obstacle drag/lift: one block per obstacle, fixed-order tree in FP64.
+__global__ void __launch_bounds__(256) k_drag(FusedArgs a) {
+  const int o = blockIdx.x;
+  if (o >= a.n_obs) return;
+  const double* link_force = a.link_force;
+  const int n_links = a.n_links;
+  const int* obs_start = a.obs_start;
+  long long slot = (*a.it_dev - 1) % a.drag_cap;
+  if (slot < 0) slot += a.drag_cap;
+  double* out = a.drag_hist + slot * 2 * a.n_obs;
+  const int l0 = obs_start[o], l1 = obs_start[o + 1];
+  double fx = 0.0, fy = 0.0;
+  for (int l = l0 + threadIdx.x; l < l1; l += blockDim.x) {
+    fx += link_force[l];
+    fy += link_force[n_links + l];
+  }
+  __shared__ double sx[256], sy[256];
+  sx[threadIdx.x] = fx;
+  sy[threadIdx.x] = fy;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sx[threadIdx.x] += sx[threadIdx.x + w];
+      sy[threadIdx.x] += sy[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[2 * o] = sx[0];
+    out[2 * o + 1] = sy[0];
+  }
+}
+
+__global__ void k_set_it(long long* it_dev, long long value) { *it_dev = value; }
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+// ev (optional): four events recorded before k_bulk, k_special, k_drag and
+// after the step, for per-kernel timing.
+template <class St, int MODE>
+static void launch_mode(const FusedArgs& a, cudaStream_t st, cudaEvent_t* ev) {
+  const int tb = 256;
+  const long long nb = (a.N + tb - 1) / tb;
+  if (ev) cudaEventRecord(ev[0], st);
+  k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
+  if (ev) cudaEventRecord(ev[1], st);
+  if (a.n_special > 0) {
+    const int ts = 128;
+    k_special<St, MODE><<<(a.n_special + ts - 1) / ts, ts, 0, st>>>(a);
+  }
+  if (ev) cudaEventRecord(ev[2], st);
+  if (MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0)
+    k_drag<<<a.n_obs, 256, 0, st>>>(a);
+  if (ev) cudaEventRecord(ev[3], st);
+}
+
+template <class St>
+static void launch_store(const FusedArgs& a, int mode, cudaStream_t st, cudaEvent_t* ev) {
+  switch (mode) {
+    case LBM_MODE_COLLIDE_FROM_G: launch_mode<St, LBM_MODE_COLLIDE_FROM_G>(a, st, ev); break;
+    case LBM_MODE_STEP: launch_mode<St, LBM_MODE_STEP>(a, st, ev); break;
+    default: launch_mode<St, LBM_MODE_FINISH>(a, st, ev); break;
+  }
+}
+
+int fused_kernels_per_step(const lbm_problem* p, int mode) {
+  int n = 1 + (p->n_special > 0 ? 1 : 0);
+  if (mode != LBM_MODE_COLLIDE_FROM_G && p->drag_hist && p->n_obstacles > 0 && p->n_links > 0) n++;
+  return n;
+}
+
+// Scratch layout: iteration counter (256 B) | stale[2][9][n_special] |
+// mac[2][3][n_special] | link_force[2][n_links]   (doubles).
+size_t fused_scratch_bytes(const lbm_problem* p) {
+  size_t ns = (size_t)(p->n_special > 0 ? p->n_special : 0);
+  size_t nl = (size_t)(p->n_links > 0 ? p->n_links : 0);
+  return 256 + sizeof(double) * (2 * 9 * ns + 2 * 3 * ns + 2 * nl) + 256;
+}
+
+static FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.N = (long long)p->nx * p->ny;
+  const double rho0 = p->precision == LBM_PREC_F64 ? 0.0 : p->rho0;
+  a.kd = make_coef<double>(p->om_p, p->om_m, rho0);
+  a.kf = make_coef<float>(p->om_p, p->om_m, rho0);
+  a.n_wall_ops = p->n_wall_ops;
+  for (int w = 0; w < 5; ++w) a.wall_ops[w] = p->wall_ops[w];
+  a.n_corner_ops = p->n_corner_ops;
+  for (int w = 0; w < 4; ++w) {
+    a.corner_ops[w] = p->corner_ops[w];
+    a.corner_nb_special[w] = p->corner_nb_special[w];
+    a.corner_special[w] = p->corner_special[w];
+  }
+  a.ibb = p->ibb;
+  a.bc_base = p->bc_base;
+  a.bc_vec = p->bc_vec;
+  a.bc_scale = p->bc_scale;
+  a.bc_scale_it0 = p->bc_scale_it0;
+  a.bc_scale_len = p->bc_scale_len;
+  a.n_special = p->n_special;
+  a.special_cell = p->special_cell;
+  a.special_link_start = p->special_link_start;
+  a.special_link_ids = p->special_link_ids;
+  a.link_cell = p->link_cell;
+  a.link_q = p->link_q;
+  a.link_nb1 = p->link_nb1;
+  a.link_nb2 = p->link_nb2;
+  a.link_p = p->link_p;
+  a.n_links = p->n_links;
+  char* base = (char*)(((uintptr_t)p->scratch + 255) & ~(uintptr_t)255);
+  a.it_dev = (long long*)base;
+  double* sc = (double*)(base + 256);
+  const size_t ns = (size_t)p->n_special;
+  a.stale[0] = sc;
+  a.stale[1] = sc + 9 * ns;
+  a.mac[0] = sc + 18 * ns;
+  a.mac[1] = sc + 21 * ns;
+  a.link_force = sc + 24 * ns;
+  a.drag_hist = p->drag_hist;
+  a.drag_cap = p->drag_cap > 0 ? p->drag_cap : 1;
+  a.n_obs = p->n_obstacles;
+  a.obs_start = p->obstacle_link_start;
+  a.rho_out = p->rho_out;
+  a.u_out = p->u_out;
+  a.g_out = p->g_out;
+  a.status = p->status_flags;
+  a.mode = mode;
+  a.advance_it = 1;
+  a.check_finite = (flags & LBM_FLAG_CHECK_FINITE) && p->status_flags ? 1 : 0;
+  a.wall_macro = (flags & LBM_FLAG_WALL_MACRO) && p->rho_out && p->u_out ? 1 : 0;
+  return a;
+}
+
+// Enqueue n_steps steps.  set_it: write it0 - 1 into the device counter first
+// (left out when a graph that must not bake the start iteration is captured).
+int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, int parity,
+                  unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev) {
+  FusedArgs a = make_args(p, mode, flags);
+  if (set_it) k_set_it<<<1, 1, 0, st>>>(a.it_dev, it0 - 1);
+  for (int k = 0; k < n_steps; ++k) {
+    const int par = (parity + k) & 1;  // f[par] holds g_up of the previous iteration
+    a.fin = p->f[par];
+    a.fout = p->f[par ^ 1];
+    a.write_macro = (flags & LBM_FLAG_MACRO_LAST) && k == n_steps - 1 && p->rho_out && p->u_out;
+    cudaEvent_t* e = ev ? ev + 4 * k : nullptr;
+    switch (p->precision) {
+      case LBM_PREC_F64: launch_store<StoreF64>(a, mode, st, e); break;
+      case LBM_PREC_F32: launch_store<StoreF32>(a, mode, st, e); break;
+      case LBM_PREC_F16S: launch_store<StoreF16>(a, mode, st, e); break;
+      default: launch_store<StoreBF16>(a, mode, st, e); break;
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("lbm_advance: launch failed: %s", cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
+}
+
+int fused_set_it(const lbm_problem* p, long long value, cudaStream_t st) {
+  char* base = (char*)(((uintptr_t)p->scratch + 255) & ~(uintptr_t)255);
+  k_set_it<<<1, 1, 0, st>>>((long long*)base, value);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("lbm_advance: launch failed: %s", cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
+}
+
+}  // namespace lbm

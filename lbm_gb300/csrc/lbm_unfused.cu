@@ -1,0 +1,352 @@
+// Kernel-level entry points: one CUDA kernel per reference function, FP64.
+//
+// These restate lbm/src/core/nb.py and lattice.macro operation by operation
+// so that an app calling the lattice methods in any order gets the reference
+// result.  This translation unit is compiled with -fmad=false: every product
+// and sum is rounded on its own as in NumPy, so the results equal the CPU
+// restatement bit for bit (division and square root are IEEE in both).
+#include "lbm_device.cuh"
+#include "lbm_internal.h"
+
+namespace lbm {
+namespace {
+
+#define IDX(q, i, j) (((long long)(q) * nx + (i)) * ny + (j))
+
+// lattice.macro, lattice.py:178-189 (sum over q in order, then divide).
+__global__ void k_macro(const double* __restrict__ g, double* __restrict__ rho,
+                        double* __restrict__ u, int nx, int ny) {
+  const long long N = (long long)nx * ny;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  double r = g[c];
+#pragma unroll
+  for (int q = 1; q < 9; ++q) r += g[q * N + c];
+  double jx = 0.0, jy = 0.0;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    jx += (double)cx(q) * g[q * N + c];
+    jy += (double)cy(q) * g[q * N + c];
+  }
+  rho[c] = r;
+  u[c] = jx / r;
+  u[N + c] = jy / r;
+}
+
+// nb_equilibrium, nb.py:7-17.
+__global__ void k_equilibrium(const double* __restrict__ u, const double* __restrict__ rho,
+                              double* __restrict__ g_eq, int nx, int ny) {
+  const long long N = (long long)nx * ny;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const double ux = u[c], uy = u[N + c];
+  const double v = 1.5 * (ux * ux + uy * uy);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const double t = 3.0 * (ux * (double)cx(q) + uy * (double)cy(q));
+    const double e = 1.0 + t + 0.5 * (t * t) - v;
+    g_eq[q * N + c] = e * (rho[c] * wgt(q));
+  }
+}
+
+// nb_col_str collision part, nb.py:24-35.
+__global__ void k_collide(const double* __restrict__ g, const double* __restrict__ g_eq,
+                          double* __restrict__ g_up, double om_p, double om_m, int nx, int ny) {
+  const long long N = (long long)nx * ny;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const double a = 1.0 - 0.5 * (om_p + om_m);
+  const double b = 0.5 * (om_p - om_m);
+  const double cc = 0.5 * (om_p + om_m);
+  g_up[c] = (1.0 - om_p) * g[c] + om_p * g_eq[c];
+#pragma unroll
+  for (int q = 1; q < 9; ++q) {
+    const int qb = opp(q);
+    g_up[q * N + c] = a * g[q * N + c] - b * g[qb * N + c] + cc * g_eq[q * N + c] +
+                      b * g_eq[qb * N + c];
+  }
+}
+
+// nb_col_str streaming part, nb.py:26 and 37-45: shift-copy on interior
+// slices, edge entries without a source untouched.
+__global__ void k_stream(double* __restrict__ g, const double* __restrict__ g_up, int nx, int ny) {
+  const long long N = (long long)nx * ny;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int i = (int)(c / ny), j = (int)(c - (long long)i * ny);
+  g[c] = g_up[c];
+#pragma unroll
+  for (int q = 1; q < 9; ++q) {
+    const int si = i - cx(q), sj = j - cy(q);
+    if (si < 0 || si >= nx || sj < 0 || sj >= ny) continue;
+    g[q * N + c] = g_up[IDX(q, si, sj)];
+  }
+}
+
+__device__ __forceinline__ int wrap(int k, int n) { return k < 0 ? k + n : k; }
+
+// nb_bounce_back_obstacle, nb.py:77-117 (one thread per link; the host keeps
+// at most one link per (cell, q)).
+__global__ void k_bounce_back(int ibb, const int32_t* __restrict__ links, long long n,
+                              const double* __restrict__ p_ibb, const double* __restrict__ g_up,
+                              double* __restrict__ g, int nx, int ny) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int i0 = links[3 * k], j0 = links[3 * k + 1], q = links[3 * k + 2];
+  if (q < 1 || q > 8) return;
+  const int qb = opp(q);
+  const int i = wrap(i0, nx), j = wrap(j0, ny);
+  if (i < 0 || i >= nx || j < 0 || j >= ny) return;  // the host rejects these links
+  if (ibb) {
+    const int im = wrap(i0 + cx(qb), nx), jm = wrap(j0 + cy(qb), ny);
+    if (im < 0 || im >= nx || jm < 0 || jm >= ny) return;
+    const double p = p_ibb[k];
+    const double pp = 2.0 * p;
+    if (p < 0.5) {
+      const int imm = wrap(i0 + 2 * cx(qb), nx), jmm = wrap(j0 + 2 * cy(qb), ny);
+      if (imm < 0 || imm >= nx || jmm < 0 || jmm >= ny) return;
+      g[IDX(qb, i, j)] = p * (pp + 1.0) * g_up[IDX(q, i, j)] +
+                         (1.0 + pp) * (1.0 - pp) * g_up[IDX(q, im, jm)] -
+                         p * (1.0 - pp) * g_up[IDX(q, imm, jmm)];
+    } else {
+      g[IDX(qb, i, j)] = (1.0 / (p * (pp + 1.0))) * g_up[IDX(q, i, j)] +
+                         ((pp - 1.0) / p) * g_up[IDX(qb, i, j)] +
+                         ((1.0 - pp) / (1.0 + pp)) * g_up[IDX(qb, im, jm)];
+    }
+  } else {
+    g[IDX(qb, i, j)] = g_up[IDX(q, i, j)];
+  }
+}
+
+// nb_drag_lift, nb.py:49-73: per-block fixed-order trees, then one block
+// sums the block partials in order.
+__global__ void k_drag_partial(const int32_t* __restrict__ links, long long n,
+                               const double* __restrict__ g_up, const double* __restrict__ g,
+                               int nx, int ny, double* __restrict__ part) {
+  __shared__ double sx[256], sy[256];
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double fx = 0.0, fy = 0.0;
+  if (k < n) {
+    const int i = wrap(links[3 * k], nx), j = wrap(links[3 * k + 1], ny), q = links[3 * k + 2];
+    if (i >= 0 && i < nx && j >= 0 && j < ny && q >= 1 && q <= 8) {
+      const double g0 = g_up[IDX(q, i, j)] + g[IDX(opp(q), i, j)];
+      fx = g0 * (double)cx(q);
+      fy = g0 * (double)cy(q);
+    }
+  }
+  sx[threadIdx.x] = fx;
+  sy[threadIdx.x] = fy;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sx[threadIdx.x] += sx[threadIdx.x + w];
+      sy[threadIdx.x] += sy[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sx[0];
+    part[2 * blockIdx.x + 1] = sy[0];
+  }
+}
+
+__global__ void k_drag_final(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double sx[256], sy[256];
+  double fx = 0.0, fy = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    fx += part[2 * b];
+    fy += part[2 * b + 1];
+  }
+  sx[threadIdx.x] = fx;
+  sy[threadIdx.x] = fy;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sx[threadIdx.x] += sx[threadIdx.x + w];
+      sy[threadIdx.x] += sy[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sx[0];
+    out[1] = sy[0];
+  }
+}
+
+// Zou-He walls: one thread per wall cell, arithmetic from lbm_device.cuh.
+__global__ void k_zou_he(int wall, double* __restrict__ u, double* __restrict__ rho,
+                         double* __restrict__ g, const double* __restrict__ vec,
+                         const double* __restrict__ rho_right, int nx, int ny) {
+  const long long N = (long long)nx * ny;
+  const bool vertical = wall == LBM_WALL_LEFT_VELOCITY || wall == LBM_WALL_RIGHT_VELOCITY ||
+                        wall == LBM_WALL_RIGHT_PRESSURE;
+  const int len = vertical ? ny : nx;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= len) return;
+  int i, j;
+  if (vertical) {
+    i = wall == LBM_WALL_LEFT_VELOCITY ? 0 : nx - 1;
+    j = t;
+  } else {
+    i = t;
+    j = wall == LBM_WALL_TOP_VELOCITY ? ny - 1 : 0;
+  }
+  const long long c = (long long)i * ny + j;
+  CellBC<double> s;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) s.g[q] = g[q * N + c];
+  s.rho = rho[c];
+  s.ux = u[c];
+  s.uy = u[N + c];
+  switch (wall) {
+    case LBM_WALL_LEFT_VELOCITY: zh_left<double>(s, vec[t], vec[len + t]); break;
+    case LBM_WALL_RIGHT_VELOCITY: zh_right<double>(s, vec[t], vec[len + t]); break;
+    case LBM_WALL_RIGHT_PRESSURE: zh_right_pressure<double>(s, rho_right[t], vec[len + t]); break;
+    case LBM_WALL_TOP_VELOCITY: zh_top<double>(s, vec[t], vec[len + t]); break;
+    default: zh_bottom<double>(s, vec[t], vec[len + t]); break;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) g[q * N + c] = s.g[q];
+  rho[c] = s.rho;
+  u[c] = s.ux;
+  u[N + c] = s.uy;
+}
+
+__global__ void k_corner(int corner, double* __restrict__ u, double* __restrict__ rho,
+                         double* __restrict__ g, int nx, int ny) {
+  const long long N = (long long)nx * ny;
+  const int lx = nx - 1, ly = ny - 1;
+  const int i = (corner == LBM_CORNER_BOTTOM_LEFT || corner == LBM_CORNER_TOP_LEFT) ? 0 : lx;
+  const int j = (corner == LBM_CORNER_BOTTOM_LEFT || corner == LBM_CORNER_BOTTOM_RIGHT) ? 0 : ly;
+  const int in = i == 0 ? 1 : lx - 1;
+  const long long c = (long long)i * ny + j, cn = (long long)in * ny + j;
+  CellBC<double> s;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) s.g[q] = g[q * N + c];
+  zh_corner<double>(corner, s, rho[cn], u[cn], u[N + cn]);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) g[q * N + c] = s.g[q];
+  rho[c] = s.rho;
+  u[c] = s.ux;
+  u[N + c] = s.uy;
+}
+
+inline unsigned blocks_for(long long n, int tb) { return (unsigned)((n + tb - 1) / tb); }
+
+int check_grid(const char* fn, int nx, int ny) {
+  if (nx < 3 || ny < 3 || (long long)nx * ny > (1LL << 31) - 1) {
+    set_error("%s: lattice %d x %d outside 3 <= n, nx*ny < 2^31", fn, nx, ny);
+    return LBM_ERR_ARG;
+  }
+  return LBM_OK;
+}
+
+}  // namespace
+}  // namespace lbm
+
+using namespace lbm;
+
+#define LBM_LAUNCH_CHECK(what)                                                      \
+  do {                                                                              \
+    cudaError_t e_ = cudaGetLastError();                                            \
+    if (e_ != cudaSuccess) {                                                        \
+      set_error("%s: %s", what, cudaGetErrorString(e_));                           \
+      return LBM_ERR_CUDA;                                                          \
+    }                                                                               \
+  } while (0)
+
+extern "C" int lbm_macro_f64(const double* g, double* rho, double* u, int nx, int ny, void* stream) {
+  if (int rc = check_grid("lbm_macro_f64", nx, ny)) return rc;
+  if (!g || !rho || !u) { set_error("lbm_macro_f64: null pointer"); return LBM_ERR_ARG; }
+  const long long N = (long long)nx * ny;
+  k_macro<<<blocks_for(N, 256), 256, 0, (cudaStream_t)stream>>>(g, rho, u, nx, ny);
+  LBM_LAUNCH_CHECK("lbm_macro_f64");
+  return LBM_OK;
+}
+
+extern "C" int lbm_equilibrium_f64(const double* u, const double* rho, double* g_eq, int nx, int ny,
+                                   void* stream) {
+  if (int rc = check_grid("lbm_equilibrium_f64", nx, ny)) return rc;
+  if (!g_eq || !rho || !u) { set_error("lbm_equilibrium_f64: null pointer"); return LBM_ERR_ARG; }
+  const long long N = (long long)nx * ny;
+  k_equilibrium<<<blocks_for(N, 256), 256, 0, (cudaStream_t)stream>>>(u, rho, g_eq, nx, ny);
+  LBM_LAUNCH_CHECK("lbm_equilibrium_f64");
+  return LBM_OK;
+}
+
+extern "C" int lbm_collision_stream_f64(double* g, const double* g_eq, double* g_up, double om_p,
+                                        double om_m, int nx, int ny, void* stream) {
+  if (int rc = check_grid("lbm_collision_stream_f64", nx, ny)) return rc;
+  if (!g || !g_eq || !g_up) { set_error("lbm_collision_stream_f64: null pointer"); return LBM_ERR_ARG; }
+  const long long N = (long long)nx * ny;
+  cudaStream_t st = (cudaStream_t)stream;
+  k_collide<<<blocks_for(N, 256), 256, 0, st>>>(g, g_eq, g_up, om_p, om_m, nx, ny);
+  k_stream<<<blocks_for(N, 256), 256, 0, st>>>(g, g_up, nx, ny);
+  LBM_LAUNCH_CHECK("lbm_collision_stream_f64");
+  return LBM_OK;
+}
+
+extern "C" int lbm_bounce_back_f64(int ibb, const int32_t* links, int64_t n, const double* p,
+                                   const double* g_up, double* g, int nx, int ny, void* stream) {
+  if (int rc = check_grid("lbm_bounce_back_f64", nx, ny)) return rc;
+  if (n < 0 || (n > 0 && (!links || !g_up || !g || (ibb && !p)))) {
+    set_error("lbm_bounce_back_f64: bad arguments (n=%lld)", (long long)n);
+    return LBM_ERR_ARG;
+  }
+  if (n == 0) return LBM_OK;
+  k_bounce_back<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(ibb, links, n, p, g_up, g, nx, ny);
+  LBM_LAUNCH_CHECK("lbm_bounce_back_f64");
+  return LBM_OK;
+}
+
+extern "C" size_t lbm_drag_lift_scratch_bytes(int64_t n) {
+  long long nb = n > 0 ? (n + 255) / 256 : 1;
+  return (size_t)(2 * nb * sizeof(double));
+}
+
+extern "C" int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* g_up, const double* g,
+                                 int nx, int ny, double* out, void* scratch, void* stream) {
+  if (int rc = check_grid("lbm_drag_lift_f64", nx, ny)) return rc;
+  if (n < 0 || !out || !scratch || (n > 0 && (!links || !g_up || !g))) {
+    set_error("lbm_drag_lift_f64: bad arguments");
+    return LBM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long nb = n > 0 ? (n + 255) / 256 : 1;
+  if (nb > (1LL << 30)) { set_error("lbm_drag_lift_f64: too many links"); return LBM_ERR_ARG; }
+  double* part = (double*)scratch;
+  k_drag_partial<<<(unsigned)nb, 256, 0, st>>>(links, n, g_up, g, nx, ny, part);
+  k_drag_final<<<1, 256, 0, st>>>(part, (int)nb, out);
+  LBM_LAUNCH_CHECK("lbm_drag_lift_f64");
+  return LBM_OK;
+}
+
+extern "C" int lbm_zou_he_f64(int wall, double* u, double* rho, double* g, const double* vec,
+                              const double* rho_right, int nx, int ny, void* stream) {
+  if (int rc = check_grid("lbm_zou_he_f64", nx, ny)) return rc;
+  if (wall < LBM_WALL_LEFT_VELOCITY || wall > LBM_WALL_BOTTOM_VELOCITY) {
+    set_error("lbm_zou_he_f64: unknown wall %d", wall);
+    return LBM_ERR_ARG;
+  }
+  if (!u || !rho || !g || !vec || (wall == LBM_WALL_RIGHT_PRESSURE && !rho_right)) {
+    set_error("lbm_zou_he_f64: null pointer");
+    return LBM_ERR_ARG;
+  }
+  const bool vertical = wall <= LBM_WALL_RIGHT_PRESSURE;
+  const int len = vertical ? ny : nx;
+  k_zou_he<<<blocks_for(len, 128), 128, 0, (cudaStream_t)stream>>>(wall, u, rho, g, vec, rho_right, nx, ny);
+  LBM_LAUNCH_CHECK("lbm_zou_he_f64");
+  return LBM_OK;
+}
+
+extern "C" int lbm_zou_he_corner_f64(int corner, double* u, double* rho, double* g, int nx, int ny,
+                                     void* stream) {
+  if (int rc = check_grid("lbm_zou_he_corner_f64", nx, ny)) return rc;
+  if (corner < 0 || corner > 3 || !u || !rho || !g) {
+    set_error("lbm_zou_he_corner_f64: bad arguments");
+    return LBM_ERR_ARG;
+  }
+  k_corner<<<1, 1, 0, (cudaStream_t)stream>>>(corner, u, rho, g, nx, ny);
+  LBM_LAUNCH_CHECK("lbm_zou_he_corner_f64");
+  return LBM_OK;
+}

@@ -1,0 +1,112 @@
+"""Whole-run parity of the GPU lattice (per-method kernels and the fused
+engine) against the reference's golden runs and the C oracle, plus the
+reference's own integration tests (lbm/tst/cavity, lbm/tst/poiseuille)."""
+import numpy as np
+import pytest
+
+from _cases import CASES, golden, make_case, max_rel, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # max relative error on f, same bar as the reference-vs-oracle tests
+# The step app at this resolution (Re 500, tau = 0.504) amplifies a 1e-16
+# relative perturbation of the initial g to 5.6e-12 after 300 iterations
+# (measured with the oracle itself), so no FP64 implementation that rounds
+# differently from the reference can agree to 1e-12 there; its bar is ten
+# times that sensitivity.
+CASE_TOL = {"step20": 6e-11}
+
+
+def check_against(out, hist, d, tol=TOL):
+    assert max_rel(out["g"], d["g"]) <= tol
+    assert max_rel(out["rho"], d["rho"]) <= tol
+    assert np.max(np.abs(out["u"] - d["u"])) <= tol * np.max(np.abs(d["u"]))
+    if "g_up" in d.files:
+        assert max_rel(out["g_up"], d["g_up"]) <= tol
+    if len(d["drag_lift"]):
+        ref = d["drag_lift"]
+        assert hist.shape == ref.shape
+        assert np.max(np.abs(hist - ref)) <= tol * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_methods_path_matches_reference(cuda, case):
+    app, n = make_case(case)
+    out, hist, _ = run_gpu(app, fused=False)
+    check_against(out, hist, golden("run_%s.npz" % case))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fused_path_matches_reference(cuda, case):
+    app, n = make_case(case)
+    out, hist, _ = run_gpu(app, fused=True)
+    check_against(out, hist, golden("run_%s.npz" % case), CASE_TOL.get(case, TOL))
+
+
+@pytest.mark.parametrize("case", ["cavity32", "turek24", "step20"])
+def test_fused_chunking_and_graphs_are_bit_identical(cuda, case):
+    a1, _ = make_case(case)
+    ref, h_ref, _ = run_gpu(a1, fused=True, chunk=1000, graph=False)
+    for chunk, graph in ((7, True), (64, True), (1, False)):
+        a2, _ = make_case(case)
+        out, h, _ = run_gpu(a2, fused=True, chunk=chunk, graph=graph)
+        for k in ("g", "g_up", "rho", "u", "g_eq"):
+            assert np.array_equal(out[k], ref[k]), (k, chunk, graph)
+        assert np.array_equal(h, h_ref)
+
+
+def test_config0_cavity200_vs_oracle(cuda):
+    """Cavity 200x200, u_lid = 0.1, Re = 100, 1000 iterations: <= 1e-12 on f."""
+    from lbm_gb300.apps import cavity
+    def mk():
+        a = cavity()
+        a.L_lbm, a.u_lbm, a.Re_lbm = 200, 0.1, 100.0
+        a.compute_lbm_parameters()
+        a.stop, a.it_max, a.output_freq = "it", 999, 10 ** 12
+        return a
+    lat, _ = run_oracle(mk())
+    out, _, _ = run_gpu(mk(), fused=True)
+    assert max_rel(out["g"], lat.g) <= TOL
+    assert max_rel(out["g_up"], lat.g_up) <= TOL
+    assert max_rel(out["rho"], lat.rho) <= TOL
+
+
+def test_reference_cavity_known_values(cuda):
+    """lbm/tst/cavity/test_cavity.py: default cavity, 4 centre-line values to 1e-6."""
+    from lbm_gb300.apps import cavity
+    app = cavity()
+    app.output_freq = 10000
+    out, _, lat = run_gpu(app, fused=True)
+    vx, uy = app.line_fields(lat)
+    assert abs(vx[10] - 0.12493089684236539) < 1.0e-6
+    assert abs(vx[50] - 0.05295104908939561) < 1.0e-6
+    assert abs(uy[10] + 0.05968571489630510) < 1.0e-6
+    assert abs(uy[50] + 0.19792323493599165) < 1.0e-6
+
+
+def test_reference_poiseuille_l1(cuda):
+    """lbm/tst/poiseuille/test_poiseuille.py: L1 error < 1e-3."""
+    from lbm_gb300.apps import poiseuille
+    app = poiseuille()
+    out, _, lat = run_gpu(app, fused=True)
+    assert app.compute_error(lat) < 1.0e-3
+
+
+def test_nonfinite_is_reported(cuda):
+    """A NaN planted in g on the host is reported as an error, not propagated silently."""
+    import lbm_gb300
+    from lbm_gb300.apps import cavity
+    import tempfile
+    app = cavity()
+    app.L_lbm = 16
+    app.compute_lbm_parameters()
+    app.it_max = 20
+    with tempfile.TemporaryDirectory() as td:
+        lat = lbm_gb300.lattice(app, output_dir=td, verbose=False)
+        app.initialize(lat)
+        g = lat.g
+        g[3, 5, 5] = np.nan
+        lat.g = g
+        from lbm_gb300.run import run_fused
+        with pytest.raises(FloatingPointError):
+            run_fused(lat, app, chunk=5)
