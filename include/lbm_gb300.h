@@ -185,6 +185,13 @@ int lbm_advance_graph(const lbm_problem* p, int64_t it0, int n_steps, int parity
  * ms_out[3] = kernels launched per step. */
 int lbm_profile_steps(const lbm_problem* p, int64_t it0, int n_steps, int parity, uint32_t flags,
                       double* ms_out, void* stream);
+/* FP64 pipe throughput of the current device: independent DFMA chains timed
+ * with CUDA events (the second roofline of the FP64 form).  Synchronises.
+ * scratch: device buffer of lbm_measure_dfma_scratch_bytes() bytes.  No
+ * counterpart in the reference (measurement helper). */
+size_t lbm_measure_dfma_scratch_bytes(void);
+int lbm_measure_dfma_rate(double* ginstr_per_s, void* scratch, size_t scratch_bytes,
+                          void* stream);
 /* Drop every cached graph (call before freeing buffers a graph refers to). */
 int lbm_graph_cache_clear(void);
 

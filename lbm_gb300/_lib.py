@@ -92,6 +92,9 @@ _SIGS = {
     "lbm_profile_steps": ([ctypes.POINTER(Problem), _i64, ctypes.c_int, ctypes.c_int,
                            ctypes.c_uint32, ctypes.POINTER(ctypes.c_double), _vp], ctypes.c_int),
     "lbm_graph_cache_clear": ([], ctypes.c_int),
+    "lbm_measure_dfma_scratch_bytes": ([], ctypes.c_size_t),
+    "lbm_measure_dfma_rate": ([ctypes.POINTER(ctypes.c_double), _vp, ctypes.c_size_t, _vp],
+                              ctypes.c_int),
     "lbm_pack_f64": ([ctypes.c_int, _vp, _vp, _i64, _d, _vp], ctypes.c_int),
     "lbm_unpack_f64": ([ctypes.c_int, _vp, _vp, _i64, _d, _vp], ctypes.c_int),
 }

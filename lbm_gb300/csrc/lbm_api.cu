@@ -252,6 +252,68 @@ extern "C" int lbm_advance_graph(const lbm_problem* p, int64_t it0, int n_steps,
   return LBM_OK;
 }
 
+// ---- FP64 pipe throughput ---------------------------------------------------------
+namespace lbm {
+namespace {
+// Eight independent FMA chains per thread, 32 DFMA per loop trip.
+__global__ void k_dfma_rate(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace
+}  // namespace lbm
+
+extern "C" int lbm_measure_dfma_rate(double* ginstr_per_s, void* scratch, size_t scratch_bytes,
+                                     void* stream) {
+  int dev = 0, sms = 0;
+  LBM_CUDA_CHECK(cudaGetDevice(&dev), "lbm_measure_dfma_rate");
+  LBM_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                 "lbm_measure_dfma_rate");
+  const int threads = 256, blocks = sms * 8, iters = 2000;
+  if (!ginstr_per_s || !scratch || scratch_bytes < (size_t)blocks * threads * sizeof(double)) {
+    set_error("lbm_measure_dfma_rate: needs %zu bytes of scratch",
+              (size_t)blocks * threads * sizeof(double));
+    return LBM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  LBM_CUDA_CHECK(cudaEventCreate(&e0), "lbm_measure_dfma_rate");
+  LBM_CUDA_CHECK(cudaEventCreate(&e1), "lbm_measure_dfma_rate");
+  float ms = 0.f;
+  cudaError_t err = cudaSuccess;
+  for (int rep = 0; rep < 3 && err == cudaSuccess; ++rep) {  // last of three (warm clocks)
+    cudaEventRecord(e0, st);
+    k_dfma_rate<<<blocks, threads, 0, st>>>((double*)scratch, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, st);
+    err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) {
+    set_error("lbm_measure_dfma_rate: %s", cudaGetErrorString(err));
+    return LBM_ERR_CUDA;
+  }
+  *ginstr_per_s = (double)blocks * threads * iters * 32.0 / (ms * 1e-3) / 1e9;
+  return LBM_OK;
+}
+
+size_t lbm_measure_dfma_scratch_bytes(void) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  return (size_t)sms * 8 * 256 * sizeof(double);
+}
+
 // ---- storage-form conversion ---------------------------------------------------
 namespace lbm {
 namespace {
