@@ -84,6 +84,20 @@ int lbm_bounce_back_f64(int ibb, const int32_t* links, int64_t n, const double* 
 size_t lbm_drag_lift_scratch_bytes(int64_t n);
 int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* g_up, const double* g,
                       int nx, int ny, double* out, void* scratch, void* stream);
+/* Same result as lbm_drag_lift_f64, for callers that cannot provide device
+ * memory (their device memory belongs to another allocator, or they must not
+ * allocate after start-up).  No counterpart in the reference.  The block
+ * partials live in a fixed 64 KiB array inside the library's device image,
+ * held by every GPU that loads the library until exit; at most
+ * LBM_DRAG_NOALLOC_MAX_LINKS links per call (more: LBM_ERR_ARG).  The first
+ * call on each device looks up the array's device address (with that device
+ * current); make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (different streams, or
+ * different host threads) race and must be serialised by the caller.
+ * Allocates nothing. */
+#define LBM_DRAG_NOALLOC_MAX_LINKS 1048576
+int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const double* g_up,
+                              const double* g, int nx, int ny, double* out, void* stream);
 /* Zou-He walls, lbm/src/core/nb.py:121-247.  wall: LBM_WALL_*; vec is the
  * wall's (2 x len) velocity vector; rho_right only for RIGHT_PRESSURE. */
 int lbm_zou_he_f64(int wall, double* u, double* rho, double* g, const double* vec,

@@ -80,6 +80,8 @@ _SIGS = {
     "lbm_drag_lift_scratch_bytes": ([_i64], ctypes.c_size_t),
     "lbm_drag_lift_f64": ([_vp, _i64, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp],
                           ctypes.c_int),
+    "lbm_drag_lift_f64_noalloc": ([_vp, _i64, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp],
+                                  ctypes.c_int),
     "lbm_zou_he_f64": ([ctypes.c_int, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp],
                        ctypes.c_int),
     "lbm_zou_he_corner_f64": ([ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp],

@@ -5,6 +5,8 @@
 // result.  This translation unit is compiled with -fmad=false: every product
 // and sum is rounded on its own as in NumPy, so the results equal the CPU
 // restatement bit for bit (division and square root are IEEE in both).
+#include <mutex>
+
 #include "lbm_device.cuh"
 #include "lbm_internal.h"
 
@@ -318,6 +320,68 @@ extern "C" int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* 
   k_drag_partial<<<(unsigned)nb, 256, 0, st>>>(links, n, g_up, g, nx, ny, part);
   k_drag_final<<<1, 256, 0, st>>>(part, (int)nb, out);
   LBM_LAUNCH_CHECK("lbm_drag_lift_f64");
+  return LBM_OK;
+}
+
+// ---- drag/lift without caller memory ------------------------------------------
+// Some callers cannot hand the library a scratch buffer: a host whose device
+// memory is owned by another allocator (a framework's caching allocator, a
+// Fortran or game-engine runtime that budgets all device memory at start-up)
+// or a real-time loop that must not allocate after set-up.  For them the
+// block partials of the drag/lift reduction live in this fixed array, part of
+// the library's device image: every GPU that loads the library holds its
+// 64 KiB until the process exits.  The host must not pass the symbol itself
+// to a kernel (on the host it names a stand-in, not device memory); its
+// device address is fetched once per device with cudaGetSymbolAddress.
+#define LBM_NOALLOC_MAX_BLOCKS (LBM_DRAG_NOALLOC_MAX_LINKS / 256)
+static __device__ __align__(256) double g_drag_noalloc_part[2 * LBM_NOALLOC_MAX_BLOCKS];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[64] = {};
+}  // namespace
+
+extern "C" int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const double* g_up,
+                                         const double* g, int nx, int ny, double* out,
+                                         void* stream) {
+  if (int rc = check_grid("lbm_drag_lift_f64_noalloc", nx, ny)) return rc;
+  if (n < 0 || !out || (n > 0 && (!links || !g_up || !g))) {
+    set_error("lbm_drag_lift_f64_noalloc: bad arguments");
+    return LBM_ERR_ARG;
+  }
+  if (n > LBM_DRAG_NOALLOC_MAX_LINKS) {
+    set_error("lbm_drag_lift_f64_noalloc: %lld links exceed the fixed scratch limit of %d links; "
+              "use lbm_drag_lift_f64 with a caller buffer",
+              (long long)n, (int)LBM_DRAG_NOALLOC_MAX_LINKS);
+    return LBM_ERR_ARG;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    set_error("lbm_drag_lift_f64_noalloc: no usable current device");
+    return LBM_ERR_CUDA;
+  }
+  double* part = nullptr;
+  {
+    // One-time set-up per device, with that device current.
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* addr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&addr, g_drag_noalloc_part);
+      if (e != cudaSuccess || !addr) {
+        set_error("lbm_drag_lift_f64_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        return LBM_ERR_CUDA;
+      }
+      g_noalloc_addr[dev] = (double*)addr;
+    }
+    part = g_noalloc_addr[dev];
+  }
+  // k_drag_partial writes all nb partials before k_drag_final reads them
+  // (same stream), so nothing from the previous call has to be cleared.
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long nb = n > 0 ? (n + 255) / 256 : 1;
+  k_drag_partial<<<(unsigned)nb, 256, 0, st>>>(links, n, g_up, g, nx, ny, part);
+  k_drag_final<<<1, 256, 0, st>>>(part, (int)nb, out);
+  LBM_LAUNCH_CHECK("lbm_drag_lift_f64_noalloc");
   return LBM_OK;
 }
 
