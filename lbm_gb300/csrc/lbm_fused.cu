@@ -122,7 +122,8 @@ __global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
   if (MODE == LBM_MODE_COLLIDE_FROM_G) {
     // Input is the full post-BC g (FP64) of every cell, edges included.
 #pragma unroll
-    for (int q = 0; q < 9; ++q) d[q] = (T)a.g_out[q * N + cell] - (St::kShift ? k.w[q] : T(0));
+    for (int q = 0; q < 9; ++q)
+      d[q] = St::kShift ? (T)(a.g_out[q * N + cell] - wgt(q) * a.kd.rho0) : (T)a.g_out[q * N + cell];
   } else {
     if (i == 0 || i == a.nx - 1 || j == 0 || j == a.ny - 1) return;
     const long long ny = a.ny;
@@ -155,11 +156,115 @@ __global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Bulk kernel, vectorised: each thread updates V consecutive cells of one
+// column (j0 .. j0+V-1, j0 a multiple of V) with one 16-byte load and one
+// 16-byte store per population plane.  Planes shifted along y (c_y = +-1)
+// need one cell beyond the thread's group: it comes from the neighbouring
+// lane's registers by a warp shuffle, or from memory for the first/last lane
+// of the warp.  Needs ny % V == 0 (groups never straddle two columns); wall
+// cells inside a group are computed with placeholder values and then
+// overwritten by k_special, as in k_bulk.
+// ---------------------------------------------------------------------------
+template <typename S, int V>
+struct alignas(sizeof(S) * V) Pack {
+  S v[V];
+};
+
+template <class St, int V>
+__global__ void __launch_bounds__(128) k_bulk_vec(FusedArgs a) {
+  using S = typename St::S;
+  using T = typename St::T;
+  using P = Pack<S, V>;
+  const long long N = a.N;
+  const int ny = a.ny;
+  const int G = ny / V;
+  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi == 0 && a.advance_it) *a.it_dev += 1;
+  const bool valid = gi < (long long)a.nx * G;
+  const int i = valid ? (int)(gi / G) : 0;
+  const int j0 = valid ? (int)(gi - (long long)i * G) * V : 0;
+  const bool active = valid && i > 0 && i < a.nx - 1;
+  const unsigned lane = threadIdx.x & 31u;
+  const S* fin = (const S*)a.fin;
+  const Coef<T>& k = coef<T>(a);
+
+  P in[9];
+  T halo[9];  // the cell just outside the group for planes with c_y != 0
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const long long base = q * N + (long long)(i - cx(q)) * ny + j0;
+    if (active) {
+      in[q] = *reinterpret_cast<const P*>(fin + base);
+    } else {
+#pragma unroll
+      for (int e = 0; e < V; ++e) in[q].v[e] = S();
+    }
+    if (cy(q) == 1) {
+      // cell j0 pulls from j0 - 1: last element of the previous lane's group
+      T h = __shfl_up_sync(0xffffffffu, (T)St::load(&in[q].v[V - 1]), 1);
+      if (lane == 0) h = (active && j0 > 0) ? St::load(fin + base - 1) : T(0);
+      halo[q] = h;
+    } else if (cy(q) == -1) {
+      // cell j0 + V - 1 pulls from j0 + V: first element of the next lane's group
+      T h = __shfl_down_sync(0xffffffffu, (T)St::load(&in[q].v[0]), 1);
+      if (lane == 31) h = (active && j0 + V < ny) ? St::load(fin + base + V) : T(0);
+      halo[q] = h;
+    } else {
+      halo[q] = T(0);
+    }
+  }
+  if (!active) return;
+
+  P out[9];
+#pragma unroll
+  for (int e = 0; e < V; ++e) {
+    T d[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      if (cy(q) == 1) {
+        d[q] = e == 0 ? halo[q] : St::load(&in[q].v[e - 1]);
+      } else if (cy(q) == -1) {
+        d[q] = e == V - 1 ? halo[q] : St::load(&in[q].v[e + 1]);
+      } else {
+        d[q] = St::load(&in[q].v[e]);
+      }
+    }
+    Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+    const long long cell = (long long)i * ny + j0 + e;
+    if (a.write_macro) {
+      a.rho_out[cell] = (double)m.rho;
+      a.u_out[cell] = (double)m.ux;
+      a.u_out[N + cell] = (double)m.uy;
+    }
+    if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
+    collide<T, St::kShift>(d, m, k);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) St::store(&out[q].v[e], d[q]);
+  }
+  S* fout = (S*)a.fout;
+#pragma unroll
+  for (int q = 0; q < 9; ++q)
+    *reinterpret_cast<P*>(fout + q * N + (long long)i * ny + j0) = out[q];
+}
+
+// ---------------------------------------------------------------------------
 // Special cells.
 // ---------------------------------------------------------------------------
-// Post-BC state of special cell s without corners (pull, links, wall ops).
+// Full (unshifted) population q from the storage form, in the form's
+// arithmetic type (no add at all for the plain FP64 form).
 template <class St>
-__device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<double>& c) {
+__device__ __forceinline__ typename St::T full_value(const typename St::S* p, int q,
+                                                     typename St::T rho0) {
+  using T = typename St::T;
+  const T v = St::load(p);
+  return St::kShift ? v + T(wgt(q)) * rho0 : v;
+}
+
+// Post-BC state of special cell s without corners (pull, links, wall ops),
+// in the storage form's arithmetic type T (FP64 for the plain form, FP32 for
+// the reduced forms).
+template <class St>
+__device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<typename St::T>& c) {
   using S = typename St::S;
   using T = typename St::T;
   const long long N = a.N;
@@ -167,7 +272,7 @@ __device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<double>
   const int cell = a.special_cell[s];
   const int i = cell / ny, j = cell - i * ny;
   const S* fin = (const S*)a.fin;
-  const double rho0 = St::kShift ? (double)a.kd.rho0 : 0.0;
+  const T rho0 = St::kShift ? T(a.kd.rho0) : T(0);
   const double* stale_in = a.stale[(it - 1) & 1];
   const double* mac_in = a.mac[(it - 1) & 1];
   const double bs = bc_scale_at(a, it - 1);
@@ -176,33 +281,33 @@ __device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<double>
   for (int q = 0; q < 9; ++q) {
     const int si = i - cx(q), sj = j - cy(q);
     if (si >= 0 && si < nx && sj >= 0 && sj < ny) {
-      c.g[q] = (double)St::load(fin + q * N + (long long)si * ny + sj) + wgt(q) * rho0;
+      c.g[q] = full_value<St>(fin + q * N + (long long)si * ny + sj, q, rho0);
     } else {
-      c.g[q] = stale_in[(long long)q * a.n_special + s];
+      c.g[q] = (T)stale_in[(long long)q * a.n_special + s];
     }
   }
-  c.rho = mac_in[s];
-  c.ux = mac_in[a.n_special + s];
-  c.uy = mac_in[2 * a.n_special + s];
+  c.rho = (T)mac_in[s];
+  c.ux = (T)mac_in[a.n_special + s];
+  c.uy = (T)mac_in[2 * a.n_special + s];
   // Obstacle links, in reference order (nb.py:77-117).
   const int l0 = a.special_link_start[s], l1 = a.special_link_start[s + 1];
   for (int l = l0; l < l1; ++l) {
     const int k = a.special_link_ids[l];
     const int q = a.link_q[k], qb = opp(q);
     const long long x = a.link_cell[k];
-    const double up_q_x = (double)St::load(fin + q * N + x) + wgt(q) * rho0;
+    const T up_q_x = full_value<St>(fin + q * N + x, q, rho0);
     if (a.ibb) {
-      const double p = a.link_p[k];
+      const T p = (T)a.link_p[k];
       const long long x1 = a.link_nb1[k];
-      if (p < 0.5) {
+      if (p < T(0.5)) {
         const long long x2 = a.link_nb2[k];
-        const double up_q_1 = (double)St::load(fin + q * N + x1) + wgt(q) * rho0;
-        const double up_q_2 = (double)St::load(fin + q * N + x2) + wgt(q) * rho0;
-        c.g[qb] = ibb_value<double>(p, up_q_x, up_q_1, up_q_2, 0.0, 0.0);
+        const T up_q_1 = full_value<St>(fin + q * N + x1, q, rho0);
+        const T up_q_2 = full_value<St>(fin + q * N + x2, q, rho0);
+        c.g[qb] = ibb_value<T>(p, up_q_x, up_q_1, up_q_2, T(0), T(0));
       } else {
-        const double up_qb_x = (double)St::load(fin + qb * N + x) + wgt(qb) * rho0;
-        const double up_qb_1 = (double)St::load(fin + qb * N + x1) + wgt(qb) * rho0;
-        c.g[qb] = ibb_value<double>(p, up_q_x, 0.0, 0.0, up_qb_x, up_qb_1);
+        const T up_qb_x = full_value<St>(fin + qb * N + x, qb, rho0);
+        const T up_qb_1 = full_value<St>(fin + qb * N + x1, qb, rho0);
+        c.g[qb] = ibb_value<T>(p, up_q_x, T(0), T(0), up_qb_x, up_qb_1);
       }
     } else {
       c.g[qb] = up_q_x;
@@ -213,19 +318,24 @@ __device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<double>
   for (int w = 0; w < a.n_wall_ops; ++w) {
     switch (a.wall_ops[w]) {
       case LBM_WALL_LEFT_VELOCITY:
-        if (i == 0) zh_left<double>(c, bc_value(a, bs, j), bc_value(a, bs, ny + j));
+        if (i == 0) zh_left<T>(c, (T)bc_value(a, bs, j), (T)bc_value(a, bs, ny + j));
         break;
       case LBM_WALL_RIGHT_VELOCITY:
-        if (i == nx - 1) zh_right<double>(c, bc_value(a, bs, off_ur + j), bc_value(a, bs, off_ur + ny + j));
+        if (i == nx - 1)
+          zh_right<T>(c, (T)bc_value(a, bs, off_ur + j), (T)bc_value(a, bs, off_ur + ny + j));
         break;
       case LBM_WALL_RIGHT_PRESSURE:
-        if (i == nx - 1) zh_right_pressure<double>(c, bc_value(a, bs, off_rr + j), bc_value(a, bs, off_ur + ny + j));
+        if (i == nx - 1)
+          zh_right_pressure<T>(c, (T)bc_value(a, bs, off_rr + j),
+                               (T)bc_value(a, bs, off_ur + ny + j));
         break;
       case LBM_WALL_TOP_VELOCITY:
-        if (j == ny - 1) zh_top<double>(c, bc_value(a, bs, off_ut + i), bc_value(a, bs, off_ut + nx + i));
+        if (j == ny - 1)
+          zh_top<T>(c, (T)bc_value(a, bs, off_ut + i), (T)bc_value(a, bs, off_ut + nx + i));
         break;
       case LBM_WALL_BOTTOM_VELOCITY:
-        if (j == 0) zh_bottom<double>(c, bc_value(a, bs, off_ub + i), bc_value(a, bs, off_ub + nx + i));
+        if (j == 0)
+          zh_bottom<T>(c, (T)bc_value(a, bs, off_ub + i), (T)bc_value(a, bs, off_ub + nx + i));
         break;
       default:
         break;
@@ -255,46 +365,42 @@ __global__ void __launch_bounds__(128) k_special(FusedArgs a) {
   const int cell = a.special_cell[s];
   const int i = cell / ny, j = cell - i * ny;
   const Coef<T>& k = coef<T>(a);
-  const double rho0 = St::kShift ? (double)a.kd.rho0 : 0.0;
+  const T rho0 = St::kShift ? T(a.kd.rho0) : T(0);
   const long long it = *a.it_dev;
-  CellBC<double> c;
+  CellBC<T> c;
   if (MODE == LBM_MODE_COLLIDE_FROM_G) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) c.g[q] = a.g_out[q * N + cell];
+    for (int q = 0; q < 9; ++q) c.g[q] = (T)a.g_out[q * N + cell];
   } else {
     bc_chain<St>(a, it, s, c);
     // Corners (nb.py:250-344): rho/u of the x-neighbour after its wall ops.
     for (int w = 0; w < a.n_corner_ops; ++w) {
       const int cn = a.corner_ops[w];
       if (a.corner_special[cn] != s) continue;
-      CellBC<double> nb;
+      CellBC<T> nb;
       bc_chain<St>(a, it, a.corner_nb_special[cn], nb);
-      zh_corner<double>(cn, c, nb.rho, nb.ux, nb.uy);
+      zh_corner<T>(cn, c, nb.rho, nb.ux, nb.uy);
     }
-    // Per-link momentum exchange terms (nb.py:49-73) with the post-BC g.
+    // Per-link momentum exchange terms (nb.py:49-73) with the post-BC g,
+    // accumulated in FP64 for every form.
     const int l0 = a.special_link_start[s], l1 = a.special_link_start[s + 1];
     const S* fin = (const S*)a.fin;
     for (int l = l0; l < l1; ++l) {
       const int kk = a.special_link_ids[l];
       const int q = a.link_q[kk];
-      const double g0 = ((double)St::load(fin + q * N + cell) + wgt(q) * rho0) + c.g[opp(q)];
+      const double g0 = (double)full_value<St>(fin + q * N + cell, q, rho0) + (double)c.g[opp(q)];
       a.link_force[kk] = g0 * (double)cx(q);
       a.link_force[a.n_links + kk] = g0 * (double)cy(q);
     }
     if (MODE == LBM_MODE_FINISH) {
 #pragma unroll
-      for (int q = 0; q < 9; ++q) a.g_out[q * N + cell] = c.g[q];
-      if (a.wall_macro && on_wall_op(a, i, j)) {
-        a.rho_out[cell] = c.rho;
-        a.u_out[cell] = c.ux;
-        a.u_out[N + cell] = c.uy;
-      }
+      for (int q = 0; q < 9; ++q) a.g_out[q * N + cell] = (double)c.g[q];
       bool corner_cell = false;
       for (int w = 0; w < a.n_corner_ops; ++w) corner_cell |= (a.corner_special[a.corner_ops[w]] == s);
-      if (a.wall_macro && corner_cell) {
-        a.rho_out[cell] = c.rho;
-        a.u_out[cell] = c.ux;
-        a.u_out[N + cell] = c.uy;
+      if (a.wall_macro && (corner_cell || on_wall_op(a, i, j))) {
+        a.rho_out[cell] = (double)c.rho;
+        a.u_out[cell] = (double)c.ux;
+        a.u_out[N + cell] = (double)c.uy;
       }
       return;
     }
@@ -303,11 +409,11 @@ __global__ void __launch_bounds__(128) k_special(FusedArgs a) {
   double* stale_out = a.stale[it & 1];
   double* mac_out = a.mac[it & 1];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) stale_out[(long long)q * a.n_special + s] = c.g[q];
+  for (int q = 0; q < 9; ++q) stale_out[(long long)q * a.n_special + s] = (double)c.g[q];
   // Macro + collision in the storage form's arithmetic.
   T d[9];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) d[q] = (T)(c.g[q] - wgt(q) * rho0);
+  for (int q = 0; q < 9; ++q) d[q] = St::kShift ? c.g[q] - T(wgt(q)) * rho0 : c.g[q];
   Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
   mac_out[s] = (double)m.rho;
   mac_out[a.n_special + s] = (double)m.ux;
@@ -368,8 +474,16 @@ template <class St, int MODE>
 static void launch_mode(const FusedArgs& a, cudaStream_t st, cudaEvent_t* ev) {
   const int tb = 256;
   const long long nb = (a.N + tb - 1) / tb;
+  // 16-byte vectors for the reduced storage forms (8 FP16/BF16 or 4 FP32 cells).
+  constexpr int kVec = 16 / (int)sizeof(typename St::S);
+  constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
   if (ev) cudaEventRecord(ev[0], st);
-  k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
+  if (kUseVec && a.ny % kVec == 0) {
+    const long long groups = (long long)a.nx * (a.ny / kVec);
+    k_bulk_vec<St, kVec><<<(unsigned)((groups + 127) / 128), 128, 0, st>>>(a);
+  } else {
+    k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
+  }
   if (ev) cudaEventRecord(ev[1], st);
   if (a.n_special > 0) {
     const int ts = 128;

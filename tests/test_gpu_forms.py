@@ -1,0 +1,81 @@
+"""Reduced-precision storage forms against the plain FP64 path.
+
+FP32, FP16-shifted and BF16-shifted storage (FP32 arithmetic) run the same
+fused kernels; their error is stated against the FP64 run of the same case.
+Bounds are about three times the errors measured on a GB300 (FP32 u L2
+3.4e-5 / 5.5e-5; FP16 2.5e-3 / 4.8e-3 with mean Cd 1.5e-4; BF16 0.099 /
+0.099 with mean Cd 1.3e-2).  The lattices have ny % 8 == 0, so the
+vectorised bulk kernel (16-byte loads, warp-shuffle halos) is the one tested.
+"""
+import numpy as np
+import pytest
+
+from _cases import run_gpu
+
+pytestmark = pytest.mark.gpu
+
+BOUNDS = {
+    # form: (cavity u L2, turek u L2, turek mean-Cd rel, turek rms-Cl rel)
+    "f32": (2e-4, 3e-4, 1e-4, 3e-4),
+    "f16s": (1e-2, 2e-2, 1e-3, 1e-2),
+    "bf16s": (0.3, 0.3, 5e-2, 0.25),
+}
+
+
+def _cavity():
+    from lbm_gb300.apps import cavity
+    a = cavity()
+    a.L_lbm, a.u_lbm = 128, 0.1
+    a.compute_lbm_parameters()
+    a.sigma = 200.0
+    a.stop, a.it_max, a.output_freq = "it", 3999, 10 ** 12
+    return a
+
+
+def _turek():
+    from lbm_gb300.apps import turek
+    a = turek()
+    a.L_lbm = 64
+    a.compute_lbm_parameters()
+    a.sigma = 500.0
+    a.stop, a.it_max, a.output_freq = "it", 5999, 10 ** 12
+    return a
+
+
+@pytest.fixture(scope="module")
+def fp64_runs(cuda):
+    return {"cavity": run_gpu(_cavity(), fused=True, precision="f64"),
+            "turek": run_gpu(_turek(), fused=True, precision="f64")}
+
+
+def _u_err(out, ref):
+    return float(np.linalg.norm(out["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
+
+
+@pytest.mark.parametrize("form", ["f32", "f16s", "bf16s"])
+def test_cavity_form_error(fp64_runs, form):
+    ref = fp64_runs["cavity"][0]
+    out, _, _ = run_gpu(_cavity(), fused=True, precision=form)
+    assert np.all(np.isfinite(out["g"]))
+    assert _u_err(out, ref) <= BOUNDS[form][0]
+
+
+@pytest.mark.parametrize("form", ["f32", "f16s", "bf16s"])
+def test_turek_form_error(fp64_runs, form):
+    ref, href, _ = fp64_runs["turek"]
+    out, h, _ = run_gpu(_turek(), fused=True, precision=form)
+    assert _u_err(out, ref) <= BOUNDS[form][1]
+    tail = slice(len(href) // 2, None)
+    cd_rel = abs(h[tail, 0].mean() - href[tail, 0].mean()) / abs(href[tail, 0].mean())
+    cl_rms = np.sqrt((h[tail, 1] ** 2).mean())
+    cl_rms_ref = np.sqrt((href[tail, 1] ** 2).mean())
+    assert cd_rel <= BOUNDS[form][2]
+    assert abs(cl_rms - cl_rms_ref) / cl_rms_ref <= BOUNDS[form][3]
+
+
+def test_reduced_forms_are_deterministic(cuda):
+    """Two FP16 runs of the same case are bit-identical (fixed-order reductions)."""
+    a, ha, _ = run_gpu(_turek(), fused=True, precision="f16s")
+    b, hb, _ = run_gpu(_turek(), fused=True, precision="f16s")
+    assert np.array_equal(a["g"], b["g"])
+    assert np.array_equal(ha, hb)
