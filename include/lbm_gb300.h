@@ -172,6 +172,13 @@ typedef struct lbm_problem {
   double* u_out;            /* [2*nx*ny] macro u                                */
   double* g_out;            /* [9*nx*ny] post-BC g (FINISH / COLLIDE_FROM_G in) */
   uint32_t* status_flags;   /* [1] device word; bit 0 = non-finite detected     */
+
+  /* Row pitch of f[0]/f[1] in elements (0 = ny).  The distributions are
+   * stored as [q][i][j] with rows of row_pitch >= ny elements; padding a
+   * row to a multiple of 16 bytes lets the bulk kernel use 16-byte vectors
+   * for any ny.  link_cell/link_nb1/link_nb2 are indices i * row_pitch + j in
+   * that layout; special_cell, g_out, rho_out and u_out use i * ny + j. */
+  int32_t row_pitch;
 } lbm_problem;
 
 /* Flags for lbm_advance. */
@@ -209,12 +216,44 @@ int lbm_measure_dfma_rate(double* ginstr_per_s, void* scratch, size_t scratch_by
 /* Drop every cached graph (call before freeing buffers a graph refers to). */
 int lbm_graph_cache_clear(void);
 
+/* ---- batched lattices ------------------------------------------------------ */
+/*
+ * Many independent lattices of one storage form advanced together: per
+ * iteration one persistent bulk kernel over a work queue of tiles of every
+ * lattice, one persistent special-cell kernel, one drag kernel.  Each
+ * lattice keeps its own buffers, tables and scratch (its lbm_problem); the
+ * batch owns the tile tables and a shared iteration counter (workspace from
+ * lbm_batch_create, released by lbm_batch_destroy).  A lattice gives the same
+ * bits in a batch as alone.  No counterpart in the reference, which runs one
+ * case per process.
+ */
+typedef struct lbm_batch lbm_batch;
+typedef struct lbm_batch_config {
+  int32_t bulk_threads;          /* threads per bulk block = groups per tile (x32) */
+  int32_t bulk_blocks_per_sm;    /* persistent bulk grid = SMs x this              */
+  int32_t special_blocks_per_sm; /* persistent special-cell grid = SMs x this      */
+  int32_t scalar_tile_cells;     /* cells per tile of lattices without 16-byte rows */
+  int32_t persistent;            /* 1: persistent blocks pull tiles from an atomic
+                                    queue; 0: one block per tile                  */
+} lbm_batch_config;
+int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32_t n_cases,
+                     const lbm_batch_config* cfg);
+int lbm_batch_destroy(lbm_batch* b);
+/* out6: lattices, bulk tiles, special tiles, drag items, SMs, kernels per step. */
+int lbm_batch_info(const lbm_batch* b, int64_t* out6);
+/* Advance every lattice by n_steps iterations (it0: first collided
+ * iteration; parity: which of each lattice's f[0]/f[1] holds the input). */
+int lbm_batch_advance(lbm_batch* b, int64_t it0, int n_steps, int parity, void* stream);
+/* Same, as a CUDA graph of n_steps iterations cached per (n_steps, parity). */
+int lbm_batch_advance_graph(lbm_batch* b, int64_t it0, int n_steps, int parity, void* stream);
+
 /* Convert distributions between the FP64 reference layout and a storage form
- * (shifted forms store f - w_q * rho0).  n_cells = nx * ny. */
-int lbm_pack_f64(int precision, const double* g, void* f, int64_t n_cells, double rho0,
+ * (shifted forms store f - w_q * rho0).  g has rows of ny, f rows of
+ * row_pitch (0 = ny); padding elements of f are left untouched. */
+int lbm_pack_f64(int precision, const double* g, void* f, int nx, int ny, int row_pitch, double rho0,
                  void* stream);
-int lbm_unpack_f64(int precision, const void* f, double* g, int64_t n_cells, double rho0,
-                   void* stream);
+int lbm_unpack_f64(int precision, const void* f, double* g, int nx, int ny, int row_pitch,
+                   double rho0, void* stream);
 
 #ifdef __cplusplus
 }

@@ -6,6 +6,7 @@ CUDA runtime:
 * ``lbm_fused.cu``   fused pull-scheme engine (all storage forms)
 * ``lbm_unfused.cu`` one kernel per reference function, ``-fmad=false``
 * ``lbm_api.cu``     C-ABI front, CUDA-graph cache, storage conversion
+* ``lbm_batch.cu``   batched lattices (persistent work-queue kernels)
 """
 import concurrent.futures
 import os
@@ -25,6 +26,7 @@ UNITS = {
     "lbm_fused.cu": [],
     "lbm_unfused.cu": ["-fmad=false"],
     "lbm_api.cu": [],
+    "lbm_batch.cu": [],
 }
 
 

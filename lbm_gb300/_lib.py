@@ -64,7 +64,16 @@ class Problem(ctypes.Structure):
         ("scratch", _vp), ("scratch_bytes", ctypes.c_size_t),
         ("drag_hist", _vp), ("drag_cap", _i64),
         ("rho_out", _vp), ("u_out", _vp), ("g_out", _vp), ("status_flags", _vp),
+        ("row_pitch", _i32),
     ]
+
+
+class BatchConfig(ctypes.Structure):
+    """Mirror of ``struct lbm_batch_config``."""
+
+    _fields_ = [("bulk_threads", _i32), ("bulk_blocks_per_sm", _i32),
+                ("special_blocks_per_sm", _i32), ("scalar_tile_cells", _i32),
+                ("persistent", _i32)]
 
 
 _SIGS = {
@@ -97,8 +106,16 @@ _SIGS = {
     "lbm_measure_dfma_scratch_bytes": ([], ctypes.c_size_t),
     "lbm_measure_dfma_rate": ([ctypes.POINTER(ctypes.c_double), _vp, ctypes.c_size_t, _vp],
                               ctypes.c_int),
-    "lbm_pack_f64": ([ctypes.c_int, _vp, _vp, _i64, _d, _vp], ctypes.c_int),
-    "lbm_unpack_f64": ([ctypes.c_int, _vp, _vp, _i64, _d, _vp], ctypes.c_int),
+    "lbm_batch_create": ([ctypes.POINTER(_vp), ctypes.POINTER(Problem), _i32,
+                          ctypes.POINTER(BatchConfig)], ctypes.c_int),
+    "lbm_batch_destroy": ([_vp], ctypes.c_int),
+    "lbm_batch_info": ([_vp, ctypes.POINTER(_i64)], ctypes.c_int),
+    "lbm_batch_advance": ([_vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
+    "lbm_batch_advance_graph": ([_vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
+    "lbm_pack_f64": ([ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _vp],
+                     ctypes.c_int),
+    "lbm_unpack_f64": ([ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d,
+                        _vp], ctypes.c_int),
 }
 
 _lib = None

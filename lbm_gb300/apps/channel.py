@@ -263,7 +263,7 @@ class obstacle_array(_channel):
     """
 
     def __init__(self, L_lbm=2048, n_grid=(20, 20), side=0.02, Re_side=2000.0, u_lbm=0.05,
-                 seed=2024, jitter=0.2, n_spts=20):
+                 seed=2024, jitter=0.2, n_spts=None):
         self.name = "obstacle_array"
         self.Re_lbm = Re_side
         self.L_lbm = L_lbm
@@ -281,6 +281,11 @@ class obstacle_array(_channel):
         self.dpi = 200
         self.side = side
         self.compute_lbm_parameters()
+        if n_spts is None:
+            # The IBB distance is measured to the nearest polygon sample
+            # (lattice.py:350-361): sample each side finer than half a cell
+            # (a side gets ceil(n_spts sqrt(side)) samples, shapes.py:104).
+            n_spts = max(4, math.ceil(side / (0.4 * self.dx) / math.sqrt(side)))
         rng = np.random.default_rng(seed)
         gx, gy = n_grid
         px = (self.x_max - self.x_min) / gx

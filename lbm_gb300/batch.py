@@ -1,0 +1,269 @@
+"""Batched sweep: many independent lattices advanced by one set of kernels.
+
+* ``sweep_apps(seed)``  the 256-case sweep: 128 lid-driven cavities with
+  n ~ U{64..512} and Re ~ U[100, 1000], 128 channels with ny ~ U{64..256},
+  nx = 4 ny, 1-6 random squares of side U[0.05, 0.15] ny and Re ~ U[100, 2000]
+  (on the channel height), all seeded from one generator.
+* ``Batch``  builds one lattice and one fused engine per app (same code as a
+  single run), gathers their C-ABI descriptions into an ``lbm_batch`` and
+  advances all of them with ``lbm_batch_advance_graph``: per iteration one
+  persistent bulk kernel over a tile work queue of every lattice, one
+  persistent special-cell kernel and one drag kernel.
+* ``autotune(batch)``  picks threads per block, persistent grid size and the
+  number of iterations per CUDA graph by timing candidates on the batch.
+"""
+import contextlib
+import ctypes
+import io
+import itertools
+import math
+import tempfile
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .apps import cavity
+from .apps.channel import _channel
+from .engine import FusedEngine, trace_bc_program
+from .lattice import lattice
+from .obstacle import obstacle
+
+
+def samples_per_side(side, dx):
+    """n_spts of generate_shape that spaces the samples of a square's side
+    (ceil(n_spts sqrt(side)) points, shapes.py:104) below 0.4 dx."""
+    return max(4, math.ceil(side / (0.4 * dx) / math.sqrt(side)))
+
+
+class channel_squares(_channel):
+    """Channel of height ny, length 4 ny, with square obstacles (cell units).
+
+    Re is defined on the channel height with the mean inlet velocity.
+    """
+
+    def __init__(self, ny, squares, Re, u_lbm=0.1, name="channel"):
+        self.name = name
+        self.Re_lbm = Re
+        self.L_lbm = ny
+        self.u_lbm = u_lbm
+        self.rho_lbm = 1.0
+        self.t_max = 1.0
+        self.x_min, self.x_max = 0.0, 4.0
+        self.y_min, self.y_max = 0.0, 1.0
+        self.IBB = True
+        self.stop = "it"
+        self.obs_cv_ct, self.obs_cv_nb = 1.0e-3, 1000
+        self.output_freq = 10 ** 12
+        self.output_it = 0
+        self.dpi = 100
+        self.compute_lbm_parameters()
+        self.obstacles = []
+        for k, (x, y, side) in enumerate(squares):
+            # The IBB distance is measured to the nearest polygon sample
+            # (lattice.py:350-361): sample each side finer than half a cell.
+            n_spts = samples_per_side(side * self.dx, self.dx)
+            self.obstacles.append(obstacle("%s_sq%d" % (name, k), 4, n_spts, "square",
+                                           side * self.dx, [x * self.dx, y * self.dx]))
+
+    def compute_lbm_parameters(self):
+        self._derive(self.L_lbm)
+
+
+def sweep_apps(seed=2024, n_cavity=128, n_channel=128):
+    """The seeded sweep of uneven cases (cavities then channels)."""
+    rng = np.random.default_rng(seed)
+    apps = []
+    for k in range(n_cavity):
+        a = cavity()
+        a.name = "cavity%d" % k
+        a.L_lbm = int(rng.integers(64, 513))
+        a.Re_lbm = float(rng.uniform(100.0, 1000.0))
+        a.u_lbm = 0.1
+        a.compute_lbm_parameters()
+        a.output_freq = 10 ** 12
+        apps.append(a)
+    for k in range(n_channel):
+        ny = int(rng.integers(64, 257))
+        nx = 4 * ny
+        n_sq = int(rng.integers(1, 7))
+        squares = []
+        tries = 0
+        while len(squares) < n_sq and tries < 1000:
+            tries += 1
+            side = float(rng.uniform(0.05, 0.15)) * ny
+            half = 0.5 * side + 4.0
+            x = float(rng.uniform(0.1 * nx + half, 0.8 * nx - half))
+            y = float(rng.uniform(half, ny - half))
+            if all(abs(x - x2) > 0.5 * (side + s2) + 6 or abs(y - y2) > 0.5 * (side + s2) + 6
+                   for (x2, y2, s2) in squares):
+                squares.append((x, y, side))
+        re = float(rng.uniform(100.0, 2000.0))
+        # At u_lbm = 0.1 channels with tau near 0.51 diverge within 10,000
+        # iterations even in FP64 (measured: tau 0.5086 at ~6,000, several at
+        # tau 0.515 between 9,500 and 10,000), so Re is clipped to keep
+        # tau >= 0.53 (Re <= 6.7 ny).
+        re = min(re, re_max_stable(ny, 0.1))
+        apps.append(channel_squares(ny, squares, re, name="channel%d" % k))
+    return apps
+
+
+def re_max_stable(ny, u_lbm, tau_min=0.53):
+    """Largest Re (on the channel height, mean inlet velocity) with tau >= tau_min."""
+    nu_min = (tau_min - 0.5) / 3.0
+    return (2.0 * u_lbm / 3.0) * ny / nu_min
+
+
+class Batch:
+    """One fused engine per app, advanced together through lbm_batch."""
+
+    def __init__(self, apps, precision="f16s", config=None, max_steps=20000, verbose=False):
+        self.apps = list(apps)
+        self.precision = precision
+        self.lattices, self.engines = [], []
+        self.tmp = tempfile.mkdtemp(prefix="lbm_batch_")
+        for a in self.apps:
+            with contextlib.redirect_stdout(io.StringIO()):
+                lat = lattice(a, precision=precision, output_dir=self.tmp, verbose=False)
+                lat.generate_image = lambda obstacles: None
+                a.initialize(lat)
+            obstacles, walls, corners = trace_bc_program(a)
+            eng = FusedEngine(lat, obstacles, walls, corners, precision=precision, drag_cap=64)
+            sched = a.bc_schedule(lat)
+            if sched is not None:
+                base, vec, scale = sched
+                eng.set_bc_schedule(base, vec, scale(np.arange(max_steps + 2)), it0=0)
+            eng.collide_from_g(0, macro=False)
+            self.lattices.append(lat)
+            self.engines.append(eng)
+        self.cells = sum(e.N for e in self.engines)
+        self.it = 1          # next iteration to collide
+        self.parity = 0      # every engine's f[0] holds g_up(0) after collide_from_g
+        self.handle = None
+        self.config = None
+        self.set_config(config or default_config())
+
+    def set_config(self, cfg):
+        if self.handle is not None:
+            _lib.call("lbm_batch_destroy", self.handle)
+            self.handle = None
+        self.config = dict(cfg)
+        arr = (_lib.Problem * len(self.engines))(*[e.P for e in self.engines])
+        c = _lib.BatchConfig(cfg["bulk_threads"], cfg["bulk_blocks_per_sm"],
+                             cfg["special_blocks_per_sm"], cfg["scalar_tile_cells"],
+                             int(cfg.get("persistent", 1)))
+        h = ctypes.c_void_p()
+        _lib.call("lbm_batch_create", ctypes.byref(h), arr, len(self.engines), ctypes.byref(c))
+        self.handle = h
+
+    def info(self):
+        out = (ctypes.c_int64 * 6)()
+        _lib.call("lbm_batch_info", self.handle, out)
+        return {"lattices": out[0], "bulk_tiles": out[1], "special_tiles": out[2],
+                "drag_items": out[3], "sms": out[4], "kernels_per_step": out[5]}
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def advance(self, n_steps, graph=True, k=None):
+        """Advance every lattice by n_steps iterations, k per graph launch."""
+        k = k or self.config.get("k_steps", 50)
+        done = 0
+        while done < n_steps:
+            n = min(k, n_steps - done)
+            fn = "lbm_batch_advance_graph" if graph else "lbm_batch_advance"
+            _lib.call(fn, self.handle, self.it, n, self.parity, self._stream())
+            self.it += n
+            self.parity ^= (n & 1)
+            done += n
+        for e in self.engines:
+            e.cur = self.parity
+
+    def check(self):
+        for e in self.engines:
+            e.check_status()
+
+    def close(self):
+        if self.handle is not None:
+            _lib.call("lbm_batch_destroy", self.handle)
+            self.handle = None
+
+
+def default_config():
+    return {"bulk_threads": 128, "bulk_blocks_per_sm": 8, "special_blocks_per_sm": 8,
+            "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 1}
+
+
+def time_batch(batch, n_steps, k=None):
+    """Device time (ms) of n_steps batched iterations."""
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    batch.advance(n_steps, graph=True, k=k)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def autotune(batch, steps=60, space=None, verbose=False):
+    """Pick the fastest batch configuration by timing candidates.
+
+    Every candidate runs ``steps`` iterations after one warm-up launch (which
+    also captures its graph); the lattices keep advancing, which does not
+    change the cost per iteration.  Returns (best config, table of trials).
+    """
+    space = space or {
+        "persistent": [1, 0],
+        "bulk_threads": [64, 128, 256],
+        "bulk_blocks_per_sm": [4, 8],
+        "special_blocks_per_sm": [8],
+        "k_steps": [50],
+    }
+    keys = list(space)
+    trials = []
+    best = None
+    for values in itertools.product(*(space[k] for k in keys)):
+        cfg = default_config()
+        cfg.update(dict(zip(keys, values)))
+        batch.set_config(cfg)
+        k = cfg["k_steps"]
+        batch.advance(k, k=k)  # warm-up + graph capture
+        n = max(k, (steps // k) * k)
+        ms = time_batch(batch, n, k=k)
+        mlups = batch.cells * n / (ms * 1e-3) / 1e6
+        trials.append((dict(cfg), mlups))
+        if verbose:
+            print(cfg, "%.0f MLUPS" % mlups)
+        if best is None or mlups > best[1]:
+            best = (dict(cfg), mlups)
+    batch.set_config(best[0])
+    return best[0], trials
+
+
+def serial_loop_mlups(batch, steps=40, graph=False):
+    """Aggregate MLUPS of advancing the same lattices one after another.
+
+    Each lattice runs ``steps`` iterations with its own fused engine and its
+    own kernel launches (three per iteration), the way a one-case-at-a-time
+    code would drive them.
+    """
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    it0 = batch.it
+    for e in batch.engines:  # warm-up (graph capture)
+        e.cur = batch.parity
+        e.steps(it0, steps, graph=graph)
+    torch.cuda.synchronize()
+    e0.record()
+    for e in batch.engines:
+        e.steps(it0 + steps, steps, graph=graph)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    # the engines moved 2*steps iterations ahead of the batch: keep them in step
+    batch.it = it0 + 2 * steps
+    batch.parity = batch.engines[0].cur
+    return batch.cells * steps / (ms * 1e-3) / 1e6, ms

@@ -21,9 +21,7 @@ void set_error(const char* fmt, ...) {
   va_end(ap);
 }
 
-namespace {
-
-int validate_problem(const lbm_problem* p, const char* fn) {
+int problem_check(const lbm_problem* p, const char* fn) {
   if (!p) { set_error("%s: null problem", fn); return LBM_ERR_ARG; }
   if (p->nx < 4 || p->ny < 4 || (long long)p->nx * p->ny > (1LL << 31) - 1) {
     set_error("%s: lattice %d x %d outside 4 <= n, nx*ny < 2^31", fn, p->nx, p->ny);
@@ -31,6 +29,11 @@ int validate_problem(const lbm_problem* p, const char* fn) {
   }
   if (p->precision < LBM_PREC_F64 || p->precision > LBM_PREC_BF16S) {
     set_error("%s: unknown precision %d", fn, p->precision);
+    return LBM_ERR_ARG;
+  }
+  if (p->row_pitch != 0 &&
+      (p->row_pitch < p->ny || (long long)p->nx * p->row_pitch > (1LL << 31) - 1)) {
+    set_error("%s: row pitch %d below ny %d or too large", fn, p->row_pitch, p->ny);
     return LBM_ERR_ARG;
   }
   if (!p->f[0] || !p->f[1] || !p->bc_base || !p->scratch) {
@@ -80,6 +83,8 @@ int validate_problem(const lbm_problem* p, const char* fn) {
   return LBM_OK;
 }
 
+namespace {
+
 // ---- CUDA-graph cache -------------------------------------------------------
 struct GraphEntry {
   lbm_problem prob;
@@ -124,7 +129,7 @@ extern "C" size_t lbm_problem_scratch_bytes(const lbm_problem* p) {
 
 extern "C" int lbm_advance(const lbm_problem* p, int mode, int64_t it0, int n_steps, int parity,
                            uint32_t flags, void* stream) {
-  if (int rc = validate_problem(p, "lbm_advance")) return rc;
+  if (int rc = problem_check(p, "lbm_advance")) return rc;
   if (mode < LBM_MODE_COLLIDE_FROM_G || mode > LBM_MODE_FINISH || n_steps < 1 ||
       (mode != LBM_MODE_STEP && n_steps != 1) || (parity != 0 && parity != 1)) {
     set_error("lbm_advance: bad mode %d / n_steps %d / parity %d", mode, n_steps, parity);
@@ -139,7 +144,7 @@ extern "C" int lbm_advance(const lbm_problem* p, int mode, int64_t it0, int n_st
 
 extern "C" int lbm_profile_steps(const lbm_problem* p, int64_t it0, int n_steps, int parity,
                                  uint32_t flags, double* ms_out, void* stream) {
-  if (int rc = validate_problem(p, "lbm_profile_steps")) return rc;
+  if (int rc = problem_check(p, "lbm_profile_steps")) return rc;
   if (n_steps < 1 || n_steps > 100000 || (parity != 0 && parity != 1) || !ms_out) {
     set_error("lbm_profile_steps: bad n_steps %d / parity %d / output", n_steps, parity);
     return LBM_ERR_ARG;
@@ -186,7 +191,7 @@ extern "C" int lbm_graph_cache_clear(void) {
 
 extern "C" int lbm_advance_graph(const lbm_problem* p, int64_t it0, int n_steps, int parity,
                                  uint32_t flags, void* stream) {
-  if (int rc = validate_problem(p, "lbm_advance_graph")) return rc;
+  if (int rc = problem_check(p, "lbm_advance_graph")) return rc;
   if (n_steps < 1 || (parity != 0 && parity != 1)) {
     set_error("lbm_advance_graph: bad n_steps %d / parity %d", n_steps, parity);
     return LBM_ERR_ARG;
@@ -317,40 +322,56 @@ size_t lbm_measure_dfma_scratch_bytes(void) {
 // ---- storage-form conversion ---------------------------------------------------
 namespace lbm {
 namespace {
+// g: FP64 reference layout [q][i][j] (rows of ny); f: storage layout (rows of
+// sy >= ny).  One thread per cell of the reference layout.
 template <class St>
-__global__ void k_pack(const double* __restrict__ g, typename St::S* __restrict__ f, long long n,
-                       double rho0) {
+__global__ void k_pack(const double* __restrict__ g, typename St::S* __restrict__ f, int nx, int ny,
+                       int sy, double rho0) {
+  const long long n = (long long)nx * ny, ns = (long long)nx * sy;
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
+  const long long i = c / ny, s = i * sy + (c - i * ny);
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
     const double v = g[q * n + c] - (St::kShift ? wgt(q) * rho0 : 0.0);
-    St::store(f + q * n + c, (typename St::T)v);
+    St::store(f + q * ns + s, (typename St::T)v);
   }
 }
 template <class St>
-__global__ void k_unpack(const typename St::S* __restrict__ f, double* __restrict__ g, long long n,
-                         double rho0) {
+__global__ void k_unpack(const typename St::S* __restrict__ f, double* __restrict__ g, int nx,
+                         int ny, int sy, double rho0) {
+  const long long n = (long long)nx * ny, ns = (long long)nx * sy;
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
+  const long long i = c / ny, s = i * sy + (c - i * ny);
 #pragma unroll
   for (int q = 0; q < 9; ++q)
-    g[q * n + c] = (double)St::load(f + q * n + c) + (St::kShift ? wgt(q) * rho0 : 0.0);
+    g[q * n + c] = (double)St::load(f + q * ns + s) + (St::kShift ? wgt(q) * rho0 : 0.0);
+}
+
+int check_conv(const char* fn, const void* g, const void* f, int nx, int ny, int sy) {
+  if (!g || !f || nx < 1 || ny < 1 || (sy != 0 && sy < ny) ||
+      (long long)nx * (sy > 0 ? sy : ny) > (1LL << 31) - 1) {
+    set_error("%s: bad arguments", fn);
+    return LBM_ERR_ARG;
+  }
+  return LBM_OK;
 }
 }  // namespace
 }  // namespace lbm
 
-extern "C" int lbm_pack_f64(int precision, const double* g, void* f, int64_t n_cells, double rho0,
-                            void* stream) {
-  if (!g || !f || n_cells <= 0) { set_error("lbm_pack_f64: bad arguments"); return LBM_ERR_ARG; }
+extern "C" int lbm_pack_f64(int precision, const double* g, void* f, int nx, int ny, int row_pitch,
+                            double rho0, void* stream) {
+  if (int rc = check_conv("lbm_pack_f64", g, f, nx, ny, row_pitch)) return rc;
+  const int sy = row_pitch > 0 ? row_pitch : ny;
   cudaStream_t st = (cudaStream_t)stream;
-  const unsigned nb = (unsigned)((n_cells + 255) / 256);
+  const unsigned nb = (unsigned)(((long long)nx * ny + 255) / 256);
   switch (precision) {
-    case LBM_PREC_F64: k_pack<StoreF64><<<nb, 256, 0, st>>>(g, (double*)f, n_cells, rho0); break;
-    case LBM_PREC_F32: k_pack<StoreF32><<<nb, 256, 0, st>>>(g, (float*)f, n_cells, rho0); break;
-    case LBM_PREC_F16S: k_pack<StoreF16><<<nb, 256, 0, st>>>(g, (__half*)f, n_cells, rho0); break;
+    case LBM_PREC_F64: k_pack<StoreF64><<<nb, 256, 0, st>>>(g, (double*)f, nx, ny, sy, rho0); break;
+    case LBM_PREC_F32: k_pack<StoreF32><<<nb, 256, 0, st>>>(g, (float*)f, nx, ny, sy, rho0); break;
+    case LBM_PREC_F16S: k_pack<StoreF16><<<nb, 256, 0, st>>>(g, (__half*)f, nx, ny, sy, rho0); break;
     case LBM_PREC_BF16S:
-      k_pack<StoreBF16><<<nb, 256, 0, st>>>(g, (__nv_bfloat16*)f, n_cells, rho0);
+      k_pack<StoreBF16><<<nb, 256, 0, st>>>(g, (__nv_bfloat16*)f, nx, ny, sy, rho0);
       break;
     default: set_error("lbm_pack_f64: unknown precision %d", precision); return LBM_ERR_ARG;
   }
@@ -358,17 +379,24 @@ extern "C" int lbm_pack_f64(int precision, const double* g, void* f, int64_t n_c
   return LBM_OK;
 }
 
-extern "C" int lbm_unpack_f64(int precision, const void* f, double* g, int64_t n_cells, double rho0,
-                              void* stream) {
-  if (!g || !f || n_cells <= 0) { set_error("lbm_unpack_f64: bad arguments"); return LBM_ERR_ARG; }
+extern "C" int lbm_unpack_f64(int precision, const void* f, double* g, int nx, int ny,
+                              int row_pitch, double rho0, void* stream) {
+  if (int rc = check_conv("lbm_unpack_f64", g, f, nx, ny, row_pitch)) return rc;
+  const int sy = row_pitch > 0 ? row_pitch : ny;
   cudaStream_t st = (cudaStream_t)stream;
-  const unsigned nb = (unsigned)((n_cells + 255) / 256);
+  const unsigned nb = (unsigned)(((long long)nx * ny + 255) / 256);
   switch (precision) {
-    case LBM_PREC_F64: k_unpack<StoreF64><<<nb, 256, 0, st>>>((const double*)f, g, n_cells, rho0); break;
-    case LBM_PREC_F32: k_unpack<StoreF32><<<nb, 256, 0, st>>>((const float*)f, g, n_cells, rho0); break;
-    case LBM_PREC_F16S: k_unpack<StoreF16><<<nb, 256, 0, st>>>((const __half*)f, g, n_cells, rho0); break;
+    case LBM_PREC_F64:
+      k_unpack<StoreF64><<<nb, 256, 0, st>>>((const double*)f, g, nx, ny, sy, rho0);
+      break;
+    case LBM_PREC_F32:
+      k_unpack<StoreF32><<<nb, 256, 0, st>>>((const float*)f, g, nx, ny, sy, rho0);
+      break;
+    case LBM_PREC_F16S:
+      k_unpack<StoreF16><<<nb, 256, 0, st>>>((const __half*)f, g, nx, ny, sy, rho0);
+      break;
     case LBM_PREC_BF16S:
-      k_unpack<StoreBF16><<<nb, 256, 0, st>>>((const __nv_bfloat16*)f, g, n_cells, rho0);
+      k_unpack<StoreBF16><<<nb, 256, 0, st>>>((const __nv_bfloat16*)f, g, nx, ny, sy, rho0);
       break;
     default: set_error("lbm_unpack_f64: unknown precision %d", precision); return LBM_ERR_ARG;
   }

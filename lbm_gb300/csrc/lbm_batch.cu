@@ -1,0 +1,361 @@
+// Batched lattices: many independent lattices (uneven sizes, Reynolds
+// numbers, geometry and boundary programs, one storage form) advanced
+// together, one iteration per three launches, each a persistent kernel
+// whose blocks pull tiles from an atomic work queue:
+//
+//   k_batch_bulk     tiles of bulk cells of every lattice (16-byte vector
+//                    groups where ny % V == 0, single cells otherwise)
+//   k_batch_special  tiles of special cells of every lattice
+//   k_batch_drag     one block per (lattice, obstacle)
+//
+// The per-cell work is the single-lattice code of lbm_fused.cuh, reading the
+// lattice's FusedArgs from a device array (one array per ping-pong parity),
+// so a lattice advanced in a batch gives the same bits as when advanced alone.
+// All lattices share one device iteration counter.
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "lbm_fused.cuh"
+
+struct lbm_batch {
+  int n_cases;
+  int precision;
+  lbm_batch_config cfg;
+  int sm_count;
+  lbm::FusedArgs* d_args;   // [2][n_cases]
+  int4* d_bulk_tiles;       // (case, first, count, vectorised)
+  int n_bulk_tiles;
+  int4* d_special_tiles;    // (case, first, count, 0)
+  int n_special_tiles;
+  int2* d_drag_items;       // (case, obstacle)
+  int n_drag_items;
+  unsigned* d_queue;        // [0] bulk queue, [1] special queue
+  long long* d_it;          // shared iteration counter
+  int any_scalar;
+  // graph cache (one per (n_steps, parity))
+  std::vector<int> g_steps, g_parity;
+  std::vector<cudaGraphExec_t> g_exec;
+};
+
+namespace lbm {
+namespace {
+
+template <class St>
+__global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict__ args,
+                                                    const int4* __restrict__ tiles, int n_tiles,
+                                                    unsigned* queue, long long* it_dev) {
+  constexpr int V = 16 / (int)sizeof(typename St::S);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *it_dev += 1;
+    queue[1] = 0;  // the special phase of this iteration starts from tile 0
+  }
+  __shared__ int t_sh;
+  for (;;) {
+    if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[0], 1u);
+    __syncthreads();
+    const int t = t_sh;
+    __syncthreads();
+    if (t >= n_tiles) break;
+    const int4 tl = tiles[t];
+    const FusedArgs& a = args[tl.x];
+    if (tl.w) {
+      // one 16-byte group per thread; tiles are blockDim groups long
+      bulk_group_vec<St, V>(a, (long long)tl.y + threadIdx.x);
+    } else {
+      for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
+        bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
+    }
+  }
+}
+
+// Same work as k_batch_bulk with one block per tile (the hardware block
+// scheduler distributes the tiles; no queue).
+template <class St>
+__global__ void __launch_bounds__(256) k_batch_bulk_grid(const FusedArgs* __restrict__ args,
+                                                         const int4* __restrict__ tiles,
+                                                         unsigned* queue, long long* it_dev) {
+  constexpr int V = 16 / (int)sizeof(typename St::S);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *it_dev += 1;
+    queue[1] = 0;
+  }
+  const int4 tl = tiles[blockIdx.x];
+  const FusedArgs& a = args[tl.x];
+  if (tl.w) {
+    bulk_group_vec<St, V>(a, (long long)tl.y + threadIdx.x);
+  } else {
+    for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
+      bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
+  }
+}
+
+template <class St>
+__global__ void __launch_bounds__(128) k_batch_special_grid(const FusedArgs* __restrict__ args,
+                                                            const int4* __restrict__ tiles,
+                                                            unsigned* queue) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;
+  const int4 tl = tiles[blockIdx.x];
+  if ((int)threadIdx.x < tl.z) special_cell<St, LBM_MODE_STEP>(args[tl.x], tl.y + threadIdx.x);
+}
+
+template <class St>
+__global__ void __launch_bounds__(128) k_batch_special(const FusedArgs* __restrict__ args,
+                                                       const int4* __restrict__ tiles, int n_tiles,
+                                                       unsigned* queue) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;  // next iteration's bulk queue
+  __shared__ int t_sh;
+  for (;;) {
+    if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[1], 1u);
+    __syncthreads();
+    const int t = t_sh;
+    __syncthreads();
+    if (t >= n_tiles) break;
+    const int4 tl = tiles[t];
+    for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
+      special_cell<St, LBM_MODE_STEP>(args[tl.x], tl.y + k);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict__ args,
+                                                    const int2* __restrict__ items, int n_items) {
+  if ((int)blockIdx.x >= n_items) return;
+  const int2 it = items[blockIdx.x];
+  drag_obstacle(args[it.x], it.y);
+}
+
+template <class St>
+void enqueue_store(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
+  const int gb = b->sm_count * b->cfg.bulk_blocks_per_sm;
+  const int gs = b->sm_count * b->cfg.special_blocks_per_sm;
+  for (int k = 0; k < n_steps; ++k) {
+    const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
+    if (b->cfg.persistent) {
+      k_batch_bulk<St><<<gb, b->cfg.bulk_threads, 0, st>>>(args, b->d_bulk_tiles,
+                                                           b->n_bulk_tiles, b->d_queue, b->d_it);
+      if (b->n_special_tiles > 0)
+        k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
+                                                b->d_queue);
+    } else {
+      k_batch_bulk_grid<St><<<b->n_bulk_tiles, b->cfg.bulk_threads, 0, st>>>(
+          args, b->d_bulk_tiles, b->d_queue, b->d_it);
+      if (b->n_special_tiles > 0)
+        k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(args, b->d_special_tiles,
+                                                                     b->d_queue);
+    }
+    if (b->n_drag_items > 0)
+      k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items);
+  }
+}
+
+int batch_enqueue(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
+  switch (b->precision) {
+    case LBM_PREC_F64: enqueue_store<StoreF64>(b, n_steps, parity, st); break;
+    case LBM_PREC_F32: enqueue_store<StoreF32>(b, n_steps, parity, st); break;
+    case LBM_PREC_F16S: enqueue_store<StoreF16>(b, n_steps, parity, st); break;
+    default: enqueue_store<StoreBF16>(b, n_steps, parity, st); break;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("lbm_batch: launch failed: %s", cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
+}
+
+__global__ void k_batch_set_it(long long* it, long long v, unsigned* queue) {
+  *it = v;
+  queue[0] = 0;
+  queue[1] = 0;
+}
+
+void batch_free(lbm_batch* b) {
+  if (!b) return;
+  for (auto e : b->g_exec) cudaGraphExecDestroy(e);
+  cudaFree(b->d_args);
+  cudaFree(b->d_bulk_tiles);
+  cudaFree(b->d_special_tiles);
+  cudaFree(b->d_drag_items);
+  cudaFree(b->d_queue);
+  cudaFree(b->d_it);
+  delete b;
+}
+
+}  // namespace
+}  // namespace lbm
+
+using namespace lbm;
+
+extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32_t n_cases,
+                                const lbm_batch_config* cfg) {
+  if (!out || !cases || n_cases < 1 || !cfg) {
+    set_error("lbm_batch_create: bad arguments");
+    return LBM_ERR_ARG;
+  }
+  *out = nullptr;
+  if (cfg->bulk_threads < 32 || cfg->bulk_threads > 256 || cfg->bulk_threads % 32 ||
+      cfg->bulk_blocks_per_sm < 1 || cfg->bulk_blocks_per_sm > 32 ||
+      cfg->special_blocks_per_sm < 1 || cfg->special_blocks_per_sm > 32 ||
+      cfg->scalar_tile_cells < 32 || cfg->scalar_tile_cells > (1 << 20) ||
+      (cfg->persistent != 0 && cfg->persistent != 1)) {
+    set_error("lbm_batch_create: bad config (threads %d, blocks/SM %d/%d, tile %d)",
+              cfg->bulk_threads, cfg->bulk_blocks_per_sm, cfg->special_blocks_per_sm,
+              cfg->scalar_tile_cells);
+    return LBM_ERR_ARG;
+  }
+  const int prec = cases[0].precision;
+  for (int c = 0; c < n_cases; ++c) {
+    if (int rc = problem_check(&cases[c], "lbm_batch_create")) return rc;
+    if (cases[c].precision != prec) {
+      set_error("lbm_batch_create: lattice %d has another storage form", c);
+      return LBM_ERR_ARG;
+    }
+  }
+  const int V = prec == LBM_PREC_F64 ? 1 : (prec == LBM_PREC_F32 ? 4 : 8);
+  std::vector<FusedArgs> args(2 * (size_t)n_cases);
+  std::vector<int4> bulk, special;
+  std::vector<int2> drag;
+  // Largest lattices first: their tiles are taken early, so the queue ends
+  // with small lattices and the last blocks finish together.
+  std::vector<int> order(n_cases);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return (long long)cases[x].nx * cases[x].ny > (long long)cases[y].nx * cases[y].ny;
+  });
+  for (int c : order) {
+    const lbm_problem& p = cases[c];
+    for (int par = 0; par < 2; ++par) {
+      FusedArgs a = make_args(&p, LBM_MODE_STEP, LBM_FLAG_CHECK_FINITE);
+      a.fin = p.f[par];
+      a.fout = p.f[par ^ 1];
+      a.advance_it = 0;
+      a.write_macro = 0;
+      args[(size_t)par * n_cases + c] = a;
+    }
+    const int sy = p.row_pitch > 0 ? p.row_pitch : p.ny;
+    const long long N = (long long)p.nx * sy;  // storage cells, padding included
+    if (V > 1 && sy % V == 0) {
+      const long long groups = (long long)p.nx * (sy / V);
+      for (long long g = 0; g < groups; g += cfg->bulk_threads)
+        bulk.push_back(make_int4(c, (int)g, (int)std::min<long long>(cfg->bulk_threads, groups - g), 1));
+    } else {
+      for (long long x = 0; x < N; x += cfg->scalar_tile_cells)
+        bulk.push_back(make_int4(c, (int)x, (int)std::min<long long>(cfg->scalar_tile_cells, N - x), 0));
+    }
+    for (int s = 0; s < p.n_special; s += 128)
+      special.push_back(make_int4(c, s, std::min(128, p.n_special - s), 0));
+    if (p.drag_hist && p.n_links > 0)
+      for (int o = 0; o < p.n_obstacles; ++o) drag.push_back(make_int2(c, o));
+  }
+  lbm_batch* b = new lbm_batch();
+  b->n_cases = n_cases;
+  b->precision = prec;
+  b->cfg = *cfg;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  b->n_bulk_tiles = (int)bulk.size();
+  b->n_special_tiles = (int)special.size();
+  b->n_drag_items = (int)drag.size();
+  cudaError_t e = cudaSuccess;
+  auto alloc_copy = [&](void** dst, const void* src, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(dst, bytes > 0 ? bytes : 16);
+    if (e == cudaSuccess && bytes > 0) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  alloc_copy((void**)&b->d_args, args.data(), args.size() * sizeof(FusedArgs));
+  alloc_copy((void**)&b->d_bulk_tiles, bulk.data(), bulk.size() * sizeof(int4));
+  alloc_copy((void**)&b->d_special_tiles, special.data(), special.size() * sizeof(int4));
+  alloc_copy((void**)&b->d_drag_items, drag.data(), drag.size() * sizeof(int2));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_queue, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(b->d_queue, 0, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_it, sizeof(long long));
+  if (e == cudaSuccess) e = cudaMemset(b->d_it, 0, sizeof(long long));
+  if (e != cudaSuccess) {
+    set_error("lbm_batch_create: %s", cudaGetErrorString(e));
+    batch_free(b);
+    return LBM_ERR_CUDA;
+  }
+  // Every lattice reads the shared counter.
+  for (auto& a : args) a.it_dev = b->d_it;
+  e = cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(FusedArgs), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_error("lbm_batch_create: %s", cudaGetErrorString(e));
+    batch_free(b);
+    return LBM_ERR_CUDA;
+  }
+  *out = b;
+  return LBM_OK;
+}
+
+extern "C" int lbm_batch_destroy(lbm_batch* b) {
+  batch_free(b);
+  return LBM_OK;
+}
+
+extern "C" int lbm_batch_info(const lbm_batch* b, int64_t* out6) {
+  if (!b || !out6) { set_error("lbm_batch_info: bad arguments"); return LBM_ERR_ARG; }
+  out6[0] = b->n_cases;
+  out6[1] = b->n_bulk_tiles;
+  out6[2] = b->n_special_tiles;
+  out6[3] = b->n_drag_items;
+  out6[4] = b->sm_count;
+  out6[5] = 1 + (b->n_special_tiles > 0 ? 1 : 0) + (b->n_drag_items > 0 ? 1 : 0);
+  return LBM_OK;
+}
+
+extern "C" int lbm_batch_advance(lbm_batch* b, int64_t it0, int n_steps, int parity,
+                                 void* stream) {
+  if (!b || n_steps < 1 || (parity != 0 && parity != 1)) {
+    set_error("lbm_batch_advance: bad arguments");
+    return LBM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  k_batch_set_it<<<1, 1, 0, st>>>(b->d_it, it0 - 1, b->d_queue);
+  return batch_enqueue(b, n_steps, parity, st);
+}
+
+extern "C" int lbm_batch_advance_graph(lbm_batch* b, int64_t it0, int n_steps, int parity,
+                                       void* stream) {
+  if (!b || n_steps < 1 || (parity != 0 && parity != 1)) {
+    set_error("lbm_batch_advance_graph: bad arguments");
+    return LBM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaGraphExec_t exec = nullptr;
+  for (size_t k = 0; k < b->g_exec.size(); ++k)
+    if (b->g_steps[k] == n_steps && b->g_parity[k] == parity) exec = b->g_exec[k];
+  if (!exec) {
+    cudaStream_t cs;
+    LBM_CUDA_CHECK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "lbm_batch_advance_graph");
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      cudaStreamDestroy(cs);
+      set_error("lbm_batch_advance_graph: begin capture: %s", cudaGetErrorString(e));
+      return LBM_ERR_CUDA;
+    }
+    int rc = batch_enqueue(b, n_steps, parity, cs);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rc != LBM_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      set_error("lbm_batch_advance_graph: %s", cudaGetErrorString(e));
+      return LBM_ERR_CUDA;
+    }
+    b->g_steps.push_back(n_steps);
+    b->g_parity.push_back(parity);
+    b->g_exec.push_back(exec);
+  }
+  k_batch_set_it<<<1, 1, 0, st>>>(b->d_it, it0 - 1, b->d_queue);
+  LBM_CUDA_CHECK(cudaGetLastError(), "lbm_batch_advance_graph");
+  LBM_CUDA_CHECK(cudaGraphLaunch(exec, st), "lbm_batch_advance_graph: launch");
+  return LBM_OK;
+}

@@ -7,6 +7,8 @@
 namespace lbm {
 // Thread-local last-error message (lbm_last_error_string).
 void set_error(const char* fmt, ...);
+// Argument checks of an lbm_problem (lbm_api.cu).
+int problem_check(const lbm_problem* p, const char* fn);
 // Fused engine (lbm_fused.cu).
 size_t fused_scratch_bytes(const lbm_problem* p);
 int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, int parity,

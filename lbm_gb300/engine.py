@@ -194,13 +194,24 @@ class FusedEngine:
         nx, ny, dev = self.nx, self.ny, self.dev
 
         st_dtype = _STORE_DTYPE[self.precision]
-        self.f = [torch.zeros((9, nx, ny), dtype=st_dtype, device=dev) for _ in range(2)]
+        # Rows of the reduced forms are padded to 16 bytes so that the bulk
+        # kernel can use 16-byte vectors whatever ny is.
+        elems = 16 // torch.tensor([], dtype=st_dtype).element_size()
+        self.sy = ny if self.precision == "f64" else -(-ny // elems) * elems
+        self.f = [torch.zeros((9, nx, self.sy), dtype=st_dtype, device=dev) for _ in range(2)]
         self.cur = 0  # f[cur] holds g_up of the last collided iteration
 
         tb = build_tables(nx, ny, self.obstacles, bool(lat.IBB))
         n_links, n_special = tb["n_links"], tb["n_special"]
         special, link_start, order = tb["special"], tb["link_start"], tb["link_ids"]
-        link_cell, lq, nb1, nb2, p = tb["link_cell"], tb["link_q"], tb["nb1"], tb["nb2"], tb["p"]
+        lq, p = tb["link_q"], tb["p"]
+
+        def storage_index(x):  # i * ny + j  ->  i * sy + j
+            x = np.asarray(x, dtype=np.int64)
+            return (x // ny) * self.sy + x % ny
+
+        link_cell = storage_index(tb["link_cell"])
+        nb1, nb2 = storage_index(tb["nb1"]), storage_index(tb["nb2"])
         starts = tb["obs_start"]
         corner_special, corner_nb = tb["corner_special"], tb["corner_nb_special"]
 
@@ -255,6 +266,7 @@ class FusedEngine:
             P.corner_special[c] = corner_special[c]
             P.corner_nb_special[c] = corner_nb[c]
         P.f[0], P.f[1] = self.f[0].data_ptr(), self.f[1].data_ptr()
+        P.row_pitch = self.sy
         P.n_special = n_special
         P.special_cell = self.t_special.data_ptr()
         P.special_link_start = self.t_link_start.data_ptr()
@@ -345,7 +357,8 @@ class FusedEngine:
     def g_up_into(self, out):
         """Unpack f[cur] (g_up of the last collided iteration) into FP64 ``out``."""
         _lib.call("lbm_unpack_f64", self.prec_id, ctypes.c_void_p(self.f[self.cur].data_ptr()),
-                  ctypes.c_void_p(out.data_ptr()), self.N, self.rho0, self._stream())
+                  ctypes.c_void_p(out.data_ptr()), self.nx, self.ny, self.sy, self.rho0,
+                  self._stream())
 
     def drag_rows(self, it_first, it_last):
         """Raw (fx, fy) per obstacle for iterations it_first..it_last (host)."""

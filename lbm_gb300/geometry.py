@@ -15,6 +15,7 @@ Two inputs of the lattice update are prepared here:
   the neighbour test, same ``np.unique`` ordering.
 """
 import math
+import warnings
 
 import numpy as np
 import scipy.special
@@ -245,6 +246,10 @@ def add_obstacle(lat, polygon, tag, ibb_on):
             dist = np.sqrt(np.square(x) + np.square(y))
             out[s:s + step] = np.min(dist, axis=1) / (lat.dx * norms[bnd[s:s + step, 2]])
         ibb = out
+        if np.any(ibb > 1.5):
+            warnings.warn("obstacle %s: %d IBB distances exceed 1.5 links (max %.2f); the polygon "
+                          "is sampled coarser than the lattice and the interpolated bounce-back "
+                          "extrapolates" % (tag, int(np.sum(ibb > 1.5)), float(ibb.max())))
 
     count = int(np.count_nonzero(mask == tag))
     area = float(np.cumsum(np.full(count, lat.dx ** 2))[-1]) if count else 0.0

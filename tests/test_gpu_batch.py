@@ -1,0 +1,70 @@
+"""Batched lattices: a lattice advanced inside a batch gives the same bits as
+the same lattice advanced alone (same per-cell code, its own tables and
+scratch), for vectorised (ny % 8 == 0) and scalar tiles, cavities and IBB
+channels, FP16-shifted and FP64 storage."""
+import numpy as np
+import pytest
+
+from lbm_gb300.apps import cavity
+from lbm_gb300.batch import Batch, channel_squares, sweep_apps
+from lbm_gb300.run import _finalize_state
+
+pytestmark = pytest.mark.gpu
+
+
+def _apps():
+    out = []
+    for n, re in ((64, 300.0), (70, 800.0), (96, 150.0)):
+        a = cavity()
+        a.L_lbm, a.Re_lbm, a.u_lbm = n, re, 0.1
+        a.compute_lbm_parameters()
+        a.sigma = 30.0
+        out.append(a)
+    out.append(channel_squares(64, [(90.0, 30.0, 8.0), (150.0, 20.0, 6.0)], 400.0))
+    out.append(channel_squares(50, [(80.0, 25.0, 7.0)], 300.0))
+    for a in out[3:]:
+        a.sigma = 30.0
+    return out
+
+
+def _finish(batch, steps):
+    res = []
+    for lat, eng in zip(batch.lattices, batch.engines):
+        eng.cur = batch.parity
+        _finalize_state(lat, eng, steps)
+        res.append((lat.g.copy(), eng.drag_rows(steps - 5, steps)))
+    return res
+
+
+@pytest.mark.parametrize("precision", ["f16s", "f64"])
+def test_batch_equals_single_lattices(cuda, precision):
+    steps = 120
+    b = Batch(_apps(), precision=precision)
+    b.advance(steps, k=40)
+    b.check()
+    got = _finish(b, steps)
+    info = b.info()
+    b.close()
+    assert info["lattices"] == 5 and info["drag_items"] == 3
+
+    s = Batch(_apps(), precision=precision)
+    for eng in s.engines:
+        eng.steps(1, steps, graph=True)
+    ref = _finish(type("B", (), {"lattices": s.lattices, "engines": s.engines,
+                                 "parity": s.engines[0].cur})(), steps)
+    s.close()
+    for (g1, d1), (g2, d2) in zip(got, ref):
+        assert np.array_equal(g1, g2)
+        assert np.array_equal(d1, d2)
+
+
+def test_sweep_generator_is_seeded_and_in_range():
+    a = sweep_apps(seed=7, n_cavity=6, n_channel=6)
+    b = sweep_apps(seed=7, n_cavity=6, n_channel=6)
+    assert [x.nx for x in a] == [x.nx for x in b]
+    for x in a[:6]:
+        assert 64 <= x.ny <= 512 and 100.0 <= x.Re_lbm <= 1000.0 and x.nx == x.ny
+    for x in a[6:]:
+        assert 64 <= x.ny <= 256 and x.nx == 4 * x.ny and 1 <= len(x.obstacles) <= 6
+        assert 100.0 <= x.Re_lbm <= 2000.0
+        assert x.tau_lbm >= 0.53 - 1e-12

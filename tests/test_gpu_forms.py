@@ -73,6 +73,21 @@ def test_turek_form_error(fp64_runs, form):
     assert abs(cl_rms - cl_rms_ref) / cl_rms_ref <= BOUNDS[form][3]
 
 
+@pytest.mark.parametrize("form", ["f32", "f16s"])
+def test_padded_rows(cuda, form):
+    """ny = 70 is not a multiple of the vector width: rows are padded to 72."""
+    def mk():
+        a = _cavity()
+        a.L_lbm = 70
+        a.compute_lbm_parameters()
+        a.sigma, a.it_max = 100.0, 1999
+        return a
+    ref, _, _ = run_gpu(mk(), fused=True, precision="f64")
+    out, _, lat = run_gpu(mk(), fused=True, precision=form)
+    assert lat._engine.sy == 72 and lat.ny == 70
+    assert _u_err(out, ref) <= BOUNDS[form][0]
+
+
 def test_reduced_forms_are_deterministic(cuda):
     """Two FP16 runs of the same case are bit-identical (fixed-order reductions)."""
     a, ha, _ = run_gpu(_turek(), fused=True, precision="f16s")
