@@ -54,6 +54,8 @@ def parse():
                     help="other storage forms measured in the same run ('' = none)")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--sweep-steps", type=int, default=10000,
+                    help="iterations of the 256-case batched sweep (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -235,6 +237,30 @@ def measure_e2e(app, lat, eng, it, steps):
             "wall_s": wall, "steps": steps}
 
 
+def measure_sweep(steps):
+    """The 256-case sweep (FP16 shifted storage): autotune, then `steps`
+    iterations of every case in batched graphs; the per-case serial launch
+    loop is timed on 20 iterations for comparison."""
+    import torch
+    from lbm_gb300.batch import Batch, autotune, serial_loop_mlups, sweep_apps, time_batch
+    t0 = time.perf_counter()
+    b = Batch(sweep_apps(seed=2024), precision="f16s", max_steps=steps + 2500)
+    setup_s = time.perf_counter() - t0
+    best, trials = autotune(b, steps=100)
+    b.check()
+    ms = time_batch(b, steps, k=best["k_steps"])
+    b.check()
+    mlups = b.cells * steps / (ms * 1e-3) / 1e6
+    serial, _ = serial_loop_mlups(b, steps=20)
+    info = b.info()
+    b.close()
+    return {"cases": info["lattices"], "cells": b.cells, "steps": steps, "mlups": mlups,
+            "ms_per_step": ms / steps, "serial_loop_mlups": serial,
+            "x_vs_serial": mlups / serial, "config": best, "setup_s": setup_s,
+            "autotune_trials": len(trials), "precision": "f16s",
+            "all_finite": True}
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (oracle port, all host threads)
 # ---------------------------------------------------------------------------
@@ -348,10 +374,17 @@ def main():
             del st
             torch.cuda.empty_cache()
 
+    sweep = None
+    if rank == 0 and args.sweep_steps > 0:
+        sweep = measure_sweep(args.sweep_steps)
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_reference(args.ny, args.cpu_seconds)
 
+    if sweep and "f16s" in forms:
+        sweep["frac_of_single_large_f16s"] = sweep["mlups"] / forms["f16s"]["mlups"]
     roof = res["roofline"]
     if traffic and traffic.get(args.precision):
         tr = traffic[args.precision]
@@ -380,7 +413,7 @@ def main():
         "roofline": roof, "second_bound": second,
         "kernel_ms": res["kernel_ms"], "e2e": e2e,
         "gpu_launches": args.steps * res["kernels_per_step"] + 1,
-        "clocks": clocks, "forms": forms, "cpu_baseline": cpu,
+        "clocks": clocks, "forms": forms, "batched_sweep": sweep, "cpu_baseline": cpu,
     }
     if rank == 0:
         print(json.dumps(line))
