@@ -247,6 +247,39 @@ int lbm_batch_advance(lbm_batch* b, int64_t it0, int n_steps, int parity, void* 
 /* Same, as a CUDA graph of n_steps iterations cached per (n_steps, parity). */
 int lbm_batch_advance_graph(lbm_batch* b, int64_t it0, int n_steps, int parity, void* stream);
 
+/* ---- adjoint (FP64) ---------------------------------------------------------- */
+/*
+ * Discrete adjoint of one fused step, for the gradient of a drag/lift
+ * objective J = sum over iterations it in [obj_it_first, obj_it_last] of
+ * sum_o (obj_w[o] fx_o(it) + obj_w[n_obstacles + o] fy_o(it)), fx/fy the raw
+ * momentum-exchange sums of nb_drag_lift (nb.py:49-73), with respect to the
+ * TRT rate om_p (om_m = 1 / (lambda / (1/om_p - 1/2) + 1/2), lambda = 1/4,
+ * lattice.py:127-131) and to every entry of the packed BC vectors.  Needs an
+ * FP64 problem whose four walls all carry a Zou-He operation and whose four
+ * corners are applied.  No counterpart in the reference (it has no gradient).
+ */
+typedef struct lbm_adjoint {
+  int64_t obj_it_first, obj_it_last;
+  const double* obj_w;          /* [2 * n_obstacles] weights of fx, then fy      */
+  const uint8_t* is_special;    /* [nx*ny] 1 for the special cells               */
+  double* adj_pulled;           /* [9*nx*ny] scratch                             */
+  double* link_adj;             /* [3*n_links] scratch                           */
+  double* corner_seed;          /* [12] scratch                                  */
+  double* grad_bc_base;         /* [4ny+4nx+ny] += dJ/d BC value                  */
+  double* grad_bc_vec;          /* [4ny+4nx+ny] += scale(it) dJ/d BC value        */
+  double* grad_omega;           /* [grad_omega_len] += per-block parts of dJ/d om_p */
+  int32_t grad_omega_len;
+} lbm_adjoint;
+size_t lbm_adjoint_omega_slots(const lbm_problem* p);
+/* Step `it` (the forward step that reads x_prev = g_up(it-1), applies the
+ * BCs and drag of iteration it-1 and collides iteration it): lam_out =
+ * dJ/dx_prev given lam_in = dJ/d g_up(it).  FP64 arrays, reference layout. */
+int lbm_adjoint_step(const lbm_problem* p, const lbm_adjoint* adj, int64_t it,
+                     const double* x_prev, const double* lam_in, double* lam_out, void* stream);
+/* First collision (from the initial g0): adds its om_p term, lam_out = dJ/dg0. */
+int lbm_adjoint_initial(const lbm_problem* p, const lbm_adjoint* adj, const double* g0,
+                        const double* lam_in, double* lam_out, void* stream);
+
 /* Convert distributions between the FP64 reference layout and a storage form
  * (shifted forms store f - w_q * rho0).  g has rows of ny, f rows of
  * row_pitch (0 = ny); padding elements of f are left untouched. */

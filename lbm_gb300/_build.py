@@ -27,6 +27,7 @@ UNITS = {
     "lbm_unfused.cu": ["-fmad=false"],
     "lbm_api.cu": [],
     "lbm_batch.cu": [],
+    "lbm_adjoint.cu": [],
 }
 
 

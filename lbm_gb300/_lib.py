@@ -76,6 +76,15 @@ class BatchConfig(ctypes.Structure):
                 ("persistent", _i32)]
 
 
+class Adjoint(ctypes.Structure):
+    """Mirror of ``struct lbm_adjoint``."""
+
+    _fields_ = [("obj_it_first", _i64), ("obj_it_last", _i64), ("obj_w", _vp),
+                ("is_special", _vp), ("adj_pulled", _vp), ("link_adj", _vp),
+                ("corner_seed", _vp), ("grad_bc_base", _vp), ("grad_bc_vec", _vp),
+                ("grad_omega", _vp), ("grad_omega_len", _i32)]
+
+
 _SIGS = {
     "lbm_abi_version": ([], ctypes.c_int),
     "lbm_last_error_string": ([], ctypes.c_char_p),
@@ -112,6 +121,11 @@ _SIGS = {
     "lbm_batch_info": ([_vp, ctypes.POINTER(_i64)], ctypes.c_int),
     "lbm_batch_advance": ([_vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
     "lbm_batch_advance_graph": ([_vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
+    "lbm_adjoint_omega_slots": ([ctypes.POINTER(Problem)], ctypes.c_size_t),
+    "lbm_adjoint_step": ([ctypes.POINTER(Problem), ctypes.POINTER(Adjoint), _i64, _vp, _vp, _vp,
+                          _vp], ctypes.c_int),
+    "lbm_adjoint_initial": ([ctypes.POINTER(Problem), ctypes.POINTER(Adjoint), _vp, _vp, _vp,
+                             _vp], ctypes.c_int),
     "lbm_pack_f64": ([ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _vp],
                      ctypes.c_int),
     "lbm_unpack_f64": ([ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d,
