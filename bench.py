@@ -38,7 +38,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_LU = {"f64": 144, "f32": 72, "f16s": 36, "bf16s": 36}
+BYTES_PER_LU = {"f64": 144, "q60": 144, "f32": 72, "f16s": 36, "bf16s": 36}
 FP64_DP_OPS_PER_LU = 67  # DP instructions of the FP64 collision (lbm_device.cuh)
 
 
@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f16s", "bf16s"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "q60", "f32", "f16s", "bf16s"])
     ap.add_argument("--ny", type=int, default=2048)
     ap.add_argument("--forms", default="f32,f16s,bf16s",
                     help="other storage forms measured in the same run ('' = none)")

@@ -27,9 +27,16 @@ int problem_check(const lbm_problem* p, const char* fn) {
     set_error("%s: lattice %d x %d outside 4 <= n, nx*ny < 2^31", fn, p->nx, p->ny);
     return LBM_ERR_ARG;
   }
-  if (p->precision < LBM_PREC_F64 || p->precision > LBM_PREC_BF16S) {
+  if (p->precision < LBM_PREC_F64 || p->precision > LBM_PREC_Q60) {
     set_error("%s: unknown precision %d", fn, p->precision);
     return LBM_ERR_ARG;
+  }
+  if (p->precision == LBM_PREC_Q60 &&
+      !(p->rho0 >= 0.75 && p->rho0 <= 1.5 && p->om_p > 0.0 && p->om_p < 2.0 && p->om_m > 0.0 &&
+        p->om_m < 2.0)) {
+    set_error("%s: the Q3.60 form needs rho0 in [0.75, 1.5] and om_p, om_m in (0, 2) "
+              "(rho0 %g, om_p %g, om_m %g)", fn, p->rho0, p->om_p, p->om_m);
+    return LBM_ERR_UNSUPPORTED;
   }
   if (p->row_pitch != 0 &&
       (p->row_pitch < p->ny || (long long)p->nx * p->row_pitch > (1LL << 31) - 1)) {
@@ -373,6 +380,7 @@ extern "C" int lbm_pack_f64(int precision, const double* g, void* f, int nx, int
     case LBM_PREC_BF16S:
       k_pack<StoreBF16><<<nb, 256, 0, st>>>(g, (__nv_bfloat16*)f, nx, ny, sy, rho0);
       break;
+    case LBM_PREC_Q60: k_pack<StoreQ60><<<nb, 256, 0, st>>>(g, (long long*)f, nx, ny, sy, rho0); break;
     default: set_error("lbm_pack_f64: unknown precision %d", precision); return LBM_ERR_ARG;
   }
   LBM_CUDA_CHECK(cudaGetLastError(), "lbm_pack_f64");
@@ -397,6 +405,9 @@ extern "C" int lbm_unpack_f64(int precision, const void* f, double* g, int nx, i
       break;
     case LBM_PREC_BF16S:
       k_unpack<StoreBF16><<<nb, 256, 0, st>>>((const __nv_bfloat16*)f, g, nx, ny, sy, rho0);
+      break;
+    case LBM_PREC_Q60:
+      k_unpack<StoreQ60><<<nb, 256, 0, st>>>((const long long*)f, g, nx, ny, sy, rho0);
       break;
     default: set_error("lbm_unpack_f64: unknown precision %d", precision); return LBM_ERR_ARG;
   }

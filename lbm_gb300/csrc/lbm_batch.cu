@@ -155,6 +155,7 @@ int batch_enqueue(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) 
     case LBM_PREC_F64: enqueue_store<StoreF64>(b, n_steps, parity, st); break;
     case LBM_PREC_F32: enqueue_store<StoreF32>(b, n_steps, parity, st); break;
     case LBM_PREC_F16S: enqueue_store<StoreF16>(b, n_steps, parity, st); break;
+    case LBM_PREC_Q60: enqueue_store<StoreQ60>(b, n_steps, parity, st); break;
     default: enqueue_store<StoreBF16>(b, n_steps, parity, st); break;
   }
   cudaError_t e = cudaGetLastError();
@@ -213,7 +214,7 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       return LBM_ERR_ARG;
     }
   }
-  const int V = prec == LBM_PREC_F64 ? 1 : (prec == LBM_PREC_F32 ? 4 : 8);
+  const int V = (prec == LBM_PREC_F64 || prec == LBM_PREC_Q60) ? 1 : (prec == LBM_PREC_F32 ? 4 : 8);
   std::vector<FusedArgs> args(2 * (size_t)n_cases);
   std::vector<int4> bulk, special;
   std::vector<int2> drag;

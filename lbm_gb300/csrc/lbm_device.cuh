@@ -50,6 +50,7 @@ struct StoreF64 {
   using S = double;
   using T = double;
   static constexpr bool kShift = false;
+  static constexpr bool kFixed = false;
   __device__ static T load(const S* p) { return *p; }
   __device__ static void store(S* p, T v) { *p = v; }
 };
@@ -57,6 +58,7 @@ struct StoreF32 {
   using S = float;
   using T = float;
   static constexpr bool kShift = true;
+  static constexpr bool kFixed = false;
   __device__ static T load(const S* p) { return *p; }
   __device__ static void store(S* p, T v) { *p = v; }
 };
@@ -64,6 +66,7 @@ struct StoreF16 {
   using S = __half;
   using T = float;
   static constexpr bool kShift = true;
+  static constexpr bool kFixed = false;
   __device__ static T load(const S* p) { return __half2float(*p); }
   __device__ static void store(S* p, T v) { *p = __float2half_rn(v); }
 };
@@ -71,9 +74,129 @@ struct StoreBF16 {
   using S = __nv_bfloat16;
   using T = float;
   static constexpr bool kShift = true;
+  static constexpr bool kFixed = false;
   __device__ static T load(const S* p) { return __bfloat162float(*p); }
   __device__ static void store(S* p, T v) { *p = __float2bfloat16_rn(v); }
 };
+
+// ---------------------------------------------------------------------------
+// 64-bit fixed point, Q3.60: a population f is held as the signed integer
+// X = round(f * 2^60), |f| < 8.  Resolution 2^-60 = 8.7e-19, finer than half
+// an FP64 ulp for every |f| >= 2^-7; sums of populations are exact.  The
+// bulk collision of this form runs on the integer pipes (collide_q60), which
+// on GB300 issue 64-bit high multiplies several times faster than the FP64
+// pipe issues DFMA.  Cells that need FP64 (walls, obstacle links) convert on
+// load and store.  kQ60Bad marks a value outside the range (NaN, Inf or
+// |f| >= 8); it converts back to NaN.
+// ---------------------------------------------------------------------------
+constexpr long long kQ60Bad = (long long)0x8000000000000000ULL;
+
+__device__ __forceinline__ long long q60_from_double(double v) {
+  if (!(fabs(v) < 8.0)) return kQ60Bad;
+  return __double2ll_rn(v * 0x1p60);
+}
+__device__ __forceinline__ double q60_to_double(long long x) {
+  if (x == kQ60Bad) return __longlong_as_double(0x7ff8000000000000LL);
+  return __ll2double_rn(x) * 0x1p-60;
+}
+
+struct StoreQ60 {
+  using S = long long;
+  using T = double;
+  static constexpr bool kShift = false;
+  static constexpr bool kFixed = true;
+  __device__ static T load(const S* p) { return q60_to_double(*p); }
+  __device__ static void store(S* p, T v) { *p = q60_from_double(v); }
+};
+
+// TRT coefficients of the Q3.60 collision as integers (host: make_coef_q60).
+// A constant c with |c| < 1/2 is stored as round(c 2^64) and applied with
+// one signed high multiply, hi(x, C) = floor(x C / 2^64); |c| < 1 as
+// round(c 2^63) applied to x << 1.
+struct CoefQ60 {
+  long long alpha;          // (1 - om_p) / 2   * 2^64
+  long long beta;           // (1 - om_m) / 2   * 2^64
+  long long a0;             // (1 - om_p)       * 2^63
+  unsigned long long wp;    // om_p w1 = om_p/9 * 2^64
+  long long wm;             // 3 om_m w1 = om_m/3 * 2^63
+  unsigned long long c1;    // 4.5 om_p w1 = om_p/2 * 2^63
+  unsigned long long third; // 1/3 * 2^64
+};
+
+// Moments and TRT collision of one cell in Q3.60, in place on x[0..8].
+// Same update as collide() above (pair form), with
+//   A_q = alpha s_q + om_p w_q P_q,  B_q = beta t_q + 3 om_m w_q c_q.j,
+//   g_up_q = A_q + B_q,  g_up_qb = A_q - B_q,  s = g_q + g_qb, t = g_q - g_qb,
+//   P_q = rho + 4.5 (c_q.j)^2/rho - 1.5 |j|^2/rho,
+// where 1/rho comes from an FP32 seed refined by one cubic step in integer
+// arithmetic.  Every product is a 64 x 64 -> high 64 multiply, truncated
+// (error below 2^-60 per product).  Returns false, leaving x undefined, when
+// the state is outside the range of the form: rho not in (9/16, 15/4), a
+// momentum component |j| >= 2, or a velocity component |u| >= 2 / (om_p/2).
+// (rho, jx, jy) are returned in Q3.60 for the macro output.
+__device__ __forceinline__ bool collide_q60(long long x[9], const CoefQ60& k, long long& rho,
+                                            long long& jx, long long& jy) {
+  typedef long long ll;
+  typedef unsigned long long ull;
+  const ll s12 = x[1] + x[2], t12 = x[1] - x[2];
+  const ll s34 = x[3] + x[4], t34 = x[3] - x[4];
+  const ll s56 = x[5] + x[6], t56 = x[5] - x[6];
+  const ll s78 = x[7] + x[8], t78 = x[7] - x[8];
+  rho = (((x[0] + s12) + s34) + s56) + s78;
+  jx = (t12 + t56) - t78;
+  jy = (t34 + t56) + t78;
+  const ll kRhoLo = 9LL << 56, kRhoHi = 15LL << 58, kTwo = 1LL << 61;
+  bool ok = (ull)(rho - kRhoLo - 1) < (ull)(kRhoHi - kRhoLo - 1);
+  ok &= (ull)(jx + kTwo - 1) < (ull)(2 * kTwo - 1);
+  ok &= (ull)(jy + kTwo - 1) < (ull)(2 * kTwo - 1);
+  if (!ok) return false;
+
+  // 1/rho in Q61 (K in (2^59, 2^62)): FP32 reciprocal of the top 32 bits of
+  // rho as the seed (about 23 bits), then K <- K (1 + e + e^2), e = 1 - rho K
+  // (Householder's third-order step), e in Q59.
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)(int)(rho >> 32)));
+  ll K = (ll)__float2uint_rn(r * 0x1p57f) << 32;
+  const ll E = (1LL << 59) - (ll)__umul64hi((ull)rho << 1, (ull)K << 1);
+  const ll Eh = E >> 18;
+  const ll C = E + (((ll)(int)Eh * (ll)(int)Eh) >> 23);
+  K += __mul64hi(K << 1, C << 4);
+
+  // c1 u = c1 j / rho (Q60), c1 = om_p / 2
+  const ll Kc = (ll)__umul64hi((ull)K << 1, k.c1);  // c1 / rho, Q61
+  const ll Ux = __mul64hi(jx << 2, Kc << 1);
+  const ll Uy = __mul64hi(jy << 2, Kc << 1);
+  ok = (ull)(Ux + kTwo - 1) < (ull)(2 * kTwo - 1);
+  ok &= (ull)(Uy + kTwo - 1) < (ull)(2 * kTwo - 1);
+  if (!ok) return false;
+  // c1 Qx, c1 Qy, c1 jx uy with Q = (c.j)(c.u)
+  const ll Tx = __mul64hi(jx << 2, Ux << 2);
+  const ll Ty = __mul64hi(jy << 2, Uy << 2);
+  const ll Txy = __mul64hi(jx << 2, Uy << 2);
+  // om_p w1 R, R = rho - 1.5 |j|^2 / rho   (1.5 om_p w1 = c1 / 3)
+  const ll WR = (ll)__umul64hi((ull)rho, k.wp) - (ll)__umul64hi((ull)(Tx + Ty), k.third);
+  // om_p w q P_q: axis pairs w1, diagonal pairs w2 = w1 / 4
+  const ll P1 = WR + Tx, P3 = WR + Ty;
+  const ll Pd = WR + Tx + Ty;
+  const ll P5 = (Pd + 2 * Txy) >> 2, P7 = (Pd - 2 * Txy) >> 2;
+  // 3 om_m w_q c_q.j
+  const ll M1 = __mul64hi(jx << 1, k.wm), M3 = __mul64hi(jy << 1, k.wm);
+  const ll M5 = (M1 + M3) >> 2, M7 = (M3 - M1) >> 2;
+  x[0] = __mul64hi(x[0] << 1, k.a0) + (WR << 2);
+#define LBM_PAIR_Q(q, qb, s, t, P, M)                   \
+  {                                                     \
+    const ll A = __mul64hi(s, k.alpha) + (P);           \
+    const ll B = __mul64hi(t, k.beta) + (M);            \
+    x[q] = A + B;                                       \
+    x[qb] = A - B;                                      \
+  }
+  LBM_PAIR_Q(1, 2, s12, t12, P1, M1)
+  LBM_PAIR_Q(3, 4, s34, t34, P3, M3)
+  LBM_PAIR_Q(5, 6, s56, t56, P5, M5)
+  LBM_PAIR_Q(7, 8, s78, t78, P7, M7)
+#undef LBM_PAIR_Q
+  return true;
+}
 
 // ---------------------------------------------------------------------------
 // TRT collision coefficients (lattice.py:127-131; nb.py:32-35 rewritten in the

@@ -19,6 +19,7 @@
 // read (nb.py:254-257), in ping-pong scratch buffers.
 #include "lbm_fused.cuh"
 
+#include <math.h>
 #include <string.h>
 
 namespace lbm {
@@ -105,6 +106,22 @@ size_t fused_scratch_bytes(const lbm_problem* p) {
   return 256 + sizeof(double) * (2 * 9 * ns + 2 * 3 * ns + 2 * nl) + 256;
 }
 
+// Integer coefficients of the Q3.60 collision, rounded from the FP64 rates
+// in extended precision (om_p, om_m in (0, 2), checked by problem_check).
+CoefQ60 make_coef_q60(double om_p, double om_m) {
+  const long double op = om_p, om = om_m;
+  auto fix = [](long double v, int e) { return (long long)llroundl(ldexpl(v, e)); };
+  CoefQ60 k;
+  k.alpha = fix((1.0L - op) / 2.0L, 64);
+  k.beta = fix((1.0L - om) / 2.0L, 64);
+  k.a0 = fix(1.0L - op, 63);
+  k.wp = (unsigned long long)fix(op / 9.0L, 64);
+  k.wm = fix(om / 3.0L, 63);
+  k.c1 = (unsigned long long)fix(op / 2.0L, 63);
+  k.third = (unsigned long long)fix(1.0L / 3.0L, 64);
+  return k;
+}
+
 FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   FusedArgs a;
   memset(&a, 0, sizeof(a));
@@ -113,9 +130,11 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.N = (long long)p->nx * p->ny;
   a.sy = p->row_pitch > 0 ? p->row_pitch : p->ny;
   a.Ns = (long long)p->nx * a.sy;
-  const double rho0 = p->precision == LBM_PREC_F64 ? 0.0 : p->rho0;
+  const bool unshifted = p->precision == LBM_PREC_F64 || p->precision == LBM_PREC_Q60;
+  const double rho0 = unshifted ? 0.0 : p->rho0;
   a.kd = make_coef<double>(p->om_p, p->om_m, rho0);
   a.kf = make_coef<float>(p->om_p, p->om_m, rho0);
+  if (p->precision == LBM_PREC_Q60) a.kq = make_coef_q60(p->om_p, p->om_m);
   a.n_wall_ops = p->n_wall_ops;
   for (int w = 0; w < 5; ++w) a.wall_ops[w] = p->wall_ops[w];
   a.n_corner_ops = p->n_corner_ops;
@@ -180,6 +199,7 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
       case LBM_PREC_F64: launch_store<StoreF64>(a, mode, st, e); break;
       case LBM_PREC_F32: launch_store<StoreF32>(a, mode, st, e); break;
       case LBM_PREC_F16S: launch_store<StoreF16>(a, mode, st, e); break;
+      case LBM_PREC_Q60: launch_store<StoreQ60>(a, mode, st, e); break;
       default: launch_store<StoreBF16>(a, mode, st, e); break;
     }
   }

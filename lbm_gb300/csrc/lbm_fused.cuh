@@ -14,6 +14,7 @@ struct FusedArgs {
   long long Ns;         // nx * sy: plane size of the distribution storage
   Coef<double> kd;
   Coef<float> kf;
+  CoefQ60 kq;
   const void* fin;
   void* fout;
   // BC program
@@ -91,10 +92,53 @@ __device__ __forceinline__ double bc_value(const FusedArgs& a, double s, int off
 // ---------------------------------------------------------------------------
 // Bulk kernel: every non-wall cell.
 // ---------------------------------------------------------------------------
+// Bulk cell of the Q3.60 form (LBM_MODE_STEP): pull the 9 integers,
+// integer collision (collide_q60), store the 9 integers.  A cell outside the
+// range of the form stores kQ60Bad (NaN when converted back) and sets status
+// bit 0 when finite checks are on.
+__device__ __forceinline__ void bulk_cell_q60(const FusedArgs& a, long long cell) {
+  const int i = (int)(cell / a.sy);
+  const int j = (int)(cell - (long long)i * a.sy);
+  if (i == 0 || i >= a.nx - 1 || j == 0 || j >= a.ny - 1) return;
+  const long long Ns = a.Ns, sy = a.sy;
+  const long long* fin = (const long long*)a.fin;
+  long long x[9];
+  x[0] = __ldg(fin + cell);
+  x[1] = __ldg(fin + 1 * Ns + cell - sy);
+  x[2] = __ldg(fin + 2 * Ns + cell + sy);
+  x[3] = __ldg(fin + 3 * Ns + cell - 1);
+  x[4] = __ldg(fin + 4 * Ns + cell + 1);
+  x[5] = __ldg(fin + 5 * Ns + cell - sy - 1);
+  x[6] = __ldg(fin + 6 * Ns + cell + sy + 1);
+  x[7] = __ldg(fin + 7 * Ns + cell + sy - 1);
+  x[8] = __ldg(fin + 8 * Ns + cell - sy + 1);
+  long long rho, jx, jy;
+  const bool ok = collide_q60(x, a.kq, rho, jx, jy);
+  if (a.write_macro) {
+    const long long rc = (long long)i * a.ny + j;
+    const double r = ok ? q60_to_double(rho) : q60_to_double(kQ60Bad);
+    a.rho_out[rc] = r;
+    a.u_out[rc] = q60_to_double(jx) / r;
+    a.u_out[a.N + rc] = q60_to_double(jy) / r;
+  }
+  if (!ok) {
+    if (a.check_finite) atomicOr(a.status, 1u);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) x[q] = kQ60Bad;
+  }
+  long long* fout = (long long*)a.fout;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) fout[q * Ns + cell] = x[q];
+}
+
 template <class St, int MODE>
 __device__ __forceinline__ void bulk_cell(const FusedArgs& a, long long cell) {
   using S = typename St::S;
   using T = typename St::T;
+  if constexpr (St::kFixed && MODE == LBM_MODE_STEP) {
+    bulk_cell_q60(a, cell);
+    return;
+  }
   // cell: index in the storage layout (i * sy + j); padding cells j >= ny
   // are skipped.  Reference-layout arrays (g_out, rho_out, u_out) use
   // rc = i * ny + j.

@@ -1,8 +1,8 @@
 """Fused engine: the per-iteration lattice update as two or three kernels.
 
 ``FusedEngine`` owns the device state of one lattice run: two ping-pong
-buffers of post-collision populations in the storage form (``f64``, ``f32``,
-``f16s``, ``bf16s``), the special-cell and link tables, the scratch that the
+buffers of post-collision populations in the storage form (``f64``, ``q60``,
+``f32``, ``f16s``, ``bf16s``), the special-cell and link tables, the scratch that the
 kernels carry from one iteration to the next, the per-iteration drag/lift
 history and the BC schedule.  It drives ``lbm_advance`` /
 ``lbm_advance_graph`` of liblbm_gb300 (include/lbm_gb300.h).
@@ -28,6 +28,7 @@ _STORE_DTYPE = {
     "f32": torch.float32,
     "f16s": torch.float16,
     "bf16s": torch.bfloat16,
+    "q60": torch.int64,
 }
 
 WALL_OPS = {
@@ -197,7 +198,7 @@ class FusedEngine:
         # Rows of the reduced forms are padded to 16 bytes so that the bulk
         # kernel can use 16-byte vectors whatever ny is.
         elems = 16 // torch.tensor([], dtype=st_dtype).element_size()
-        self.sy = ny if self.precision == "f64" else -(-ny // elems) * elems
+        self.sy = ny if self.precision in ("f64", "q60") else -(-ny // elems) * elems
         self.f = [torch.zeros((9, nx, self.sy), dtype=st_dtype, device=dev) for _ in range(2)]
         self.cur = 0  # f[cur] holds g_up of the last collided iteration
 

@@ -36,26 +36,35 @@ def test_methods_path_matches_reference(cuda, case):
     check_against(out, hist, golden("run_%s.npz" % case))
 
 
+# The plain path in its two forms: FP64 storage and arithmetic ("f64"), and
+# 64-bit fixed-point storage with the bulk collision on the integer pipes
+# ("q60").  Both are held to the same bars.
+PLAIN = ["f64", "q60"]
+
+
+@pytest.mark.parametrize("precision", PLAIN)
 @pytest.mark.parametrize("case", CASES)
-def test_fused_path_matches_reference(cuda, case):
+def test_fused_path_matches_reference(cuda, case, precision):
     app, n = make_case(case)
-    out, hist, _ = run_gpu(app, fused=True)
+    out, hist, _ = run_gpu(app, fused=True, precision=precision)
     check_against(out, hist, golden("run_%s.npz" % case), CASE_TOL.get(case, TOL))
 
 
+@pytest.mark.parametrize("precision", PLAIN)
 @pytest.mark.parametrize("case", ["cavity32", "turek24", "step20"])
-def test_fused_chunking_and_graphs_are_bit_identical(cuda, case):
+def test_fused_chunking_and_graphs_are_bit_identical(cuda, case, precision):
     a1, _ = make_case(case)
-    ref, h_ref, _ = run_gpu(a1, fused=True, chunk=1000, graph=False)
+    ref, h_ref, _ = run_gpu(a1, fused=True, chunk=1000, graph=False, precision=precision)
     for chunk, graph in ((7, True), (64, True), (1, False)):
         a2, _ = make_case(case)
-        out, h, _ = run_gpu(a2, fused=True, chunk=chunk, graph=graph)
+        out, h, _ = run_gpu(a2, fused=True, chunk=chunk, graph=graph, precision=precision)
         for k in ("g", "g_up", "rho", "u", "g_eq"):
             assert np.array_equal(out[k], ref[k]), (k, chunk, graph)
         assert np.array_equal(h, h_ref)
 
 
-def test_config0_cavity200_vs_oracle(cuda):
+@pytest.mark.parametrize("precision", PLAIN)
+def test_config0_cavity200_vs_oracle(cuda, precision):
     """Cavity 200x200, u_lid = 0.1, Re = 100, 1000 iterations: <= 1e-12 on f."""
     from lbm_gb300.apps import cavity
     def mk():
@@ -65,7 +74,7 @@ def test_config0_cavity200_vs_oracle(cuda):
         a.stop, a.it_max, a.output_freq = "it", 999, 10 ** 12
         return a
     lat, _ = run_oracle(mk())
-    out, _, _ = run_gpu(mk(), fused=True)
+    out, _, _ = run_gpu(mk(), fused=True, precision=precision)
     assert max_rel(out["g"], lat.g) <= TOL
     assert max_rel(out["g_up"], lat.g_up) <= TOL
     assert max_rel(out["rho"], lat.rho) <= TOL
@@ -92,20 +101,25 @@ def test_reference_poiseuille_l1(cuda):
     assert app.compute_error(lat) < 1.0e-3
 
 
-def test_nonfinite_is_reported(cuda):
-    """A NaN planted in g on the host is reported as an error, not propagated silently."""
+@pytest.mark.parametrize("precision", PLAIN)
+@pytest.mark.parametrize("bad", [np.nan, 50.0])
+def test_nonfinite_is_reported(cuda, precision, bad):
+    """A NaN (or, for the fixed-point form, a value outside its range) planted
+    in g on the host is reported as an error, not propagated silently."""
     import lbm_gb300
     from lbm_gb300.apps import cavity
     import tempfile
+    if precision == "f64" and np.isfinite(bad):
+        pytest.skip("a large finite value is a valid FP64 state")
     app = cavity()
     app.L_lbm = 16
     app.compute_lbm_parameters()
     app.it_max = 20
     with tempfile.TemporaryDirectory() as td:
-        lat = lbm_gb300.lattice(app, output_dir=td, verbose=False)
+        lat = lbm_gb300.lattice(app, output_dir=td, verbose=False, precision=precision)
         app.initialize(lat)
         g = lat.g
-        g[3, 5, 5] = np.nan
+        g[3, 5, 5] = bad
         lat.g = g
         from lbm_gb300.run import run_fused
         with pytest.raises(FloatingPointError):
