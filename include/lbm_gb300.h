@@ -38,12 +38,13 @@ extern "C" {
 #define LBM_PREC_F32 1   /* FP32 storage of f - w*rho0, FP32 arithmetic              */
 #define LBM_PREC_F16S 2  /* FP16 storage of f - w*rho0, FP32 arithmetic              */
 #define LBM_PREC_BF16S 3 /* BF16 storage of f - w*rho0, FP32 arithmetic              */
-/* 64-bit fixed-point storage of f (Q3.60: f * 2^60 as int64, |f| < 8; resolution
- * 2^-60, sums exact) with the bulk collision in integer arithmetic and FP64 at
- * wall and link cells.  Needs rho0 in [3/4, 3/2] and om_p, om_m in (0, 2);
- * a cell whose rho leaves (9/16, 15/4) or whose |j| or |u| leaves the range is
- * reported like a non-finite value and stored as INT64_MIN, which unpacks to
- * NaN.  No counterpart in the reference (its FP64 path computes in FP64). */
+/* 64-bit fixed-point storage of f (Q3.60: f * 2^60 as int64, |f| < 8;
+ * resolution 2^-60, sums exact) with the bulk collision in integer arithmetic
+ * and FP64 at wall and link cells.  Needs rho0 in [3/4, 3/2] and om_p, om_m in
+ * [1/1024, 1.999]; a cell whose rho leaves (9/16, 15/4) or whose |j| or |u|
+ * leaves the range is reported like a non-finite value and stored as
+ * INT64_MIN, which unpacks to NaN.  No counterpart in the reference (its FP64
+ * path computes in FP64). */
 #define LBM_PREC_Q60 4
 
 /* Wall operations (Zou-He), lbm/src/core/nb.py:121-247. */

@@ -32,9 +32,9 @@ int problem_check(const lbm_problem* p, const char* fn) {
     return LBM_ERR_ARG;
   }
   if (p->precision == LBM_PREC_Q60 &&
-      !(p->rho0 >= 0.75 && p->rho0 <= 1.5 && p->om_p > 0.0 && p->om_p < 2.0 && p->om_m > 0.0 &&
-        p->om_m < 2.0)) {
-    set_error("%s: the Q3.60 form needs rho0 in [0.75, 1.5] and om_p, om_m in (0, 2) "
+      !(p->rho0 >= 0.75 && p->rho0 <= 1.5 && p->om_p >= 1.0 / 1024 && p->om_p <= 1.999 &&
+        p->om_m >= 1.0 / 1024 && p->om_m <= 1.999)) {
+    set_error("%s: the Q3.60 form needs rho0 in [0.75, 1.5] and om_p, om_m in [1/1024, 1.999] "
               "(rho0 %g, om_p %g, om_m %g)", fn, p->rho0, p->om_p, p->om_m);
     return LBM_ERR_UNSUPPORTED;
   }

@@ -109,18 +109,38 @@ struct StoreQ60 {
   __device__ static void store(S* p, T v) { *p = q60_from_double(v); }
 };
 
-// TRT coefficients of the Q3.60 collision as integers (host: make_coef_q60).
-// A constant c with |c| < 1/2 is stored as round(c 2^64) and applied with
-// one signed high multiply, hi(x, C) = floor(x C / 2^64); |c| < 1 as
-// round(c 2^63) applied to x << 1.
+// Signed 64 x 64 -> high 64 multiply from three 32 x 32 -> 64 products.
+// x = h 2^32 + l with both halves signed 32-bit (split); then
+//   x y / 2^64 = xh yh + (xh yl + xl yh) / 2^32 + xl yl / 2^64,
+// and mul_hi drops the last term and floors the middle one: the result is
+// within (-1/4, 5/4) of x y / 2^64 for |x|, |y| < 2^62.  Three IMAD.WIDE
+// instead of the longer unsigned-product-plus-sign-correction sequence of
+// mul.hi.s64.
+struct Split {
+  int h, l;
+};
+__host__ __device__ __forceinline__ Split split(long long x) {
+  Split s;
+  s.l = (int)(unsigned)x;
+  s.h = (int)(x >> 32) + (int)((unsigned)x >> 31);
+  return s;
+}
+__device__ __forceinline__ long long mul_hi(Split x, Split y) {
+  const long long cross = (long long)x.h * y.l + (long long)x.l * y.h;
+  return (long long)x.h * y.h + (cross >> 32);
+}
+
+// TRT coefficients of the Q3.60 collision as split integers (host:
+// make_coef_q60).  A constant c with |c| < 1/2 is stored as round(c 2^64)
+// and applied as mul_hi(x, C); |c| < 1 as round(c 2^63) applied to x << 1.
 struct CoefQ60 {
-  long long alpha;          // (1 - om_p) / 2   * 2^64
-  long long beta;           // (1 - om_m) / 2   * 2^64
-  long long a0;             // (1 - om_p)       * 2^63
-  unsigned long long wp;    // om_p w1 = om_p/9 * 2^64
-  long long wm;             // 3 om_m w1 = om_m/3 * 2^63
-  unsigned long long c1;    // 4.5 om_p w1 = om_p/2 * 2^63
-  unsigned long long third; // 1/3 * 2^64
+  Split alpha;   // (1 - om_p) / 2   * 2^64
+  Split beta;    // (1 - om_m) / 2   * 2^64
+  Split a0;      // (1 - om_p)       * 2^63
+  Split wp;      // om_p w1 = om_p/9 * 2^64
+  Split wm;      // 3 om_m w1 = om_m/3 * 2^63
+  Split c1;      // 4.5 om_p w1 = om_p/2 * 2^63
+  Split third;   // 1/3 * 2^64
 };
 
 // Moments and TRT collision of one cell in Q3.60, in place on x[0..8].
@@ -129,11 +149,11 @@ struct CoefQ60 {
 //   g_up_q = A_q + B_q,  g_up_qb = A_q - B_q,  s = g_q + g_qb, t = g_q - g_qb,
 //   P_q = rho + 4.5 (c_q.j)^2/rho - 1.5 |j|^2/rho,
 // where 1/rho comes from an FP32 seed refined by one cubic step in integer
-// arithmetic.  Every product is a 64 x 64 -> high 64 multiply, truncated
-// (error below 2^-60 per product).  Returns false, leaving x undefined, when
-// the state is outside the range of the form: rho not in (9/16, 15/4), a
-// momentum component |j| >= 2, or a velocity component |u| >= 2 / (om_p/2).
-// (rho, jx, jy) are returned in Q3.60 for the macro output.
+// arithmetic.  Every product is a mul_hi (error below 1.25 units of 2^-60).
+// Returns false, leaving x undefined, when the state is outside the range of
+// the form: rho not in (9/16, 15/4), a momentum component |j| >= 3/2, or a
+// velocity component |u| >= 3 / om_p.  (rho, jx, jy) are returned in
+// Q3.60 for the macro output.
 __device__ __forceinline__ bool collide_q60(long long x[9], const CoefQ60& k, long long& rho,
                                             long long& jx, long long& jy) {
   typedef long long ll;
@@ -145,10 +165,11 @@ __device__ __forceinline__ bool collide_q60(long long x[9], const CoefQ60& k, lo
   rho = (((x[0] + s12) + s34) + s56) + s78;
   jx = (t12 + t56) - t78;
   jy = (t34 + t56) + t78;
-  const ll kRhoLo = 9LL << 56, kRhoHi = 15LL << 58, kTwo = 1LL << 61;
+  // Range of the form (keeps every operand of mul_hi below 2^63 - 2^32).
+  const ll kRhoLo = 9LL << 56, kRhoHi = 15LL << 58, kJ = 3LL << 59;
   bool ok = (ull)(rho - kRhoLo - 1) < (ull)(kRhoHi - kRhoLo - 1);
-  ok &= (ull)(jx + kTwo - 1) < (ull)(2 * kTwo - 1);
-  ok &= (ull)(jy + kTwo - 1) < (ull)(2 * kTwo - 1);
+  ok &= (ull)(jx + kJ - 1) < (ull)(2 * kJ - 1);
+  ok &= (ull)(jy + kJ - 1) < (ull)(2 * kJ - 1);
   if (!ok) return false;
 
   // 1/rho in Q61 (K in (2^59, 2^62)): FP32 reciprocal of the top 32 bits of
@@ -156,37 +177,42 @@ __device__ __forceinline__ bool collide_q60(long long x[9], const CoefQ60& k, lo
   // (Householder's third-order step), e in Q59.
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)(int)(rho >> 32)));
-  ll K = (ll)__float2uint_rn(r * 0x1p57f) << 32;
-  const ll E = (1LL << 59) - (ll)__umul64hi((ull)rho << 1, (ull)K << 1);
+  const unsigned K0 = __float2uint_rn(r * 0x1p57f);  // 1/rho in Q29
+  // rho K0 in Q59: (rho << 2) K0 / 2^32 as a 64 x 32 product, low word floored
+  const ull rho2 = (ull)rho << 2;
+  const ll rK = (ll)((rho2 >> 32) * K0 + (((rho2 & 0xffffffffULL) * K0) >> 32));
+  const ll E = (1LL << 59) - rK;
   const ll Eh = E >> 18;
   const ll C = E + (((ll)(int)Eh * (ll)(int)Eh) >> 23);
-  K += __mul64hi(K << 1, C << 4);
+  const ll K = ((ll)K0 << 32) + mul_hi(split((ll)K0 << 33), split(C << 4));
 
   // c1 u = c1 j / rho (Q60), c1 = om_p / 2
-  const ll Kc = (ll)__umul64hi((ull)K << 1, k.c1);  // c1 / rho, Q61
-  const ll Ux = __mul64hi(jx << 2, Kc << 1);
-  const ll Uy = __mul64hi(jy << 2, Kc << 1);
-  ok = (ull)(Ux + kTwo - 1) < (ull)(2 * kTwo - 1);
-  ok &= (ull)(Uy + kTwo - 1) < (ull)(2 * kTwo - 1);
+  const Split jx2 = split(jx << 2), jy2 = split(jy << 2);
+  const Split Kc = split(mul_hi(split(K << 1), k.c1) << 1);  // c1 / rho, Q62
+  const ll Ux = mul_hi(jx2, Kc);
+  const ll Uy = mul_hi(jy2, Kc);
+  ok = (ull)(Ux + kJ - 1) < (ull)(2 * kJ - 1);
+  ok &= (ull)(Uy + kJ - 1) < (ull)(2 * kJ - 1);
   if (!ok) return false;
   // c1 Qx, c1 Qy, c1 jx uy with Q = (c.j)(c.u)
-  const ll Tx = __mul64hi(jx << 2, Ux << 2);
-  const ll Ty = __mul64hi(jy << 2, Uy << 2);
-  const ll Txy = __mul64hi(jx << 2, Uy << 2);
+  const Split Uy2 = split(Uy << 2);
+  const ll Tx = mul_hi(jx2, split(Ux << 2));
+  const ll Ty = mul_hi(jy2, Uy2);
+  const ll Txy = mul_hi(jx2, Uy2);
   // om_p w1 R, R = rho - 1.5 |j|^2 / rho   (1.5 om_p w1 = c1 / 3)
-  const ll WR = (ll)__umul64hi((ull)rho, k.wp) - (ll)__umul64hi((ull)(Tx + Ty), k.third);
+  const ll WR = mul_hi(split(rho), k.wp) - mul_hi(split(Tx + Ty), k.third);
   // om_p w q P_q: axis pairs w1, diagonal pairs w2 = w1 / 4
   const ll P1 = WR + Tx, P3 = WR + Ty;
   const ll Pd = WR + Tx + Ty;
   const ll P5 = (Pd + 2 * Txy) >> 2, P7 = (Pd - 2 * Txy) >> 2;
   // 3 om_m w_q c_q.j
-  const ll M1 = __mul64hi(jx << 1, k.wm), M3 = __mul64hi(jy << 1, k.wm);
+  const ll M1 = mul_hi(split(jx << 1), k.wm), M3 = mul_hi(split(jy << 1), k.wm);
   const ll M5 = (M1 + M3) >> 2, M7 = (M3 - M1) >> 2;
-  x[0] = __mul64hi(x[0] << 1, k.a0) + (WR << 2);
+  x[0] = mul_hi(split(x[0] << 1), k.a0) + (WR << 2);
 #define LBM_PAIR_Q(q, qb, s, t, P, M)                   \
   {                                                     \
-    const ll A = __mul64hi(s, k.alpha) + (P);           \
-    const ll B = __mul64hi(t, k.beta) + (M);            \
+    const ll A = mul_hi(split(s), k.alpha) + (P);       \
+    const ll B = mul_hi(split(t), k.beta) + (M);        \
     x[q] = A + B;                                       \
     x[qb] = A - B;                                      \
   }

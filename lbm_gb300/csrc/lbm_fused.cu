@@ -39,6 +39,15 @@ __global__ void __launch_bounds__(128) k_bulk_vec(FusedArgs a) {
   bulk_group_vec<St, V>(a, gi);
 }
 
+// Q3.60 bulk kernel: block b covers column i = b / jb, rows
+// j = (b mod jb) * 256 + threadIdx.x (block-uniform index arithmetic).
+__global__ void __launch_bounds__(256) k_bulk_q60(FusedArgs a, int jb) {
+  const int i = blockIdx.x / jb;
+  const int j = (blockIdx.x - i * jb) * 256 + threadIdx.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.advance_it) *a.it_dev += 1;
+  bulk_q60_ij(a, i, j);
+}
+
 template <class St, int MODE>
 __global__ void __launch_bounds__(128) k_special(FusedArgs a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -66,7 +75,10 @@ static void launch_mode(const FusedArgs& a, cudaStream_t st, cudaEvent_t* ev) {
   constexpr int kVec = 16 / (int)sizeof(typename St::S);
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
   if (ev) cudaEventRecord(ev[0], st);
-  if (kUseVec && a.sy % kVec == 0) {
+  if (St::kFixed && MODE == LBM_MODE_STEP) {
+    const int jb = (a.ny + 255) / 256;
+    k_bulk_q60<<<(unsigned)((long long)a.nx * jb), 256, 0, st>>>(a, jb);
+  } else if (kUseVec && a.sy % kVec == 0) {
     const long long groups = (long long)a.nx * (a.sy / kVec);
     k_bulk_vec<St, kVec><<<(unsigned)((groups + 127) / 128), 128, 0, st>>>(a);
   } else {
@@ -107,18 +119,19 @@ size_t fused_scratch_bytes(const lbm_problem* p) {
 }
 
 // Integer coefficients of the Q3.60 collision, rounded from the FP64 rates
-// in extended precision (om_p, om_m in (0, 2), checked by problem_check).
+// in extended precision (om_p, om_m in [1/1024, 1.999], checked by
+// problem_check, keep every split half inside 32 bits).
 CoefQ60 make_coef_q60(double om_p, double om_m) {
   const long double op = om_p, om = om_m;
-  auto fix = [](long double v, int e) { return (long long)llroundl(ldexpl(v, e)); };
+  auto fix = [](long double v, int e) { return split((long long)llroundl(ldexpl(v, e))); };
   CoefQ60 k;
   k.alpha = fix((1.0L - op) / 2.0L, 64);
   k.beta = fix((1.0L - om) / 2.0L, 64);
   k.a0 = fix(1.0L - op, 63);
-  k.wp = (unsigned long long)fix(op / 9.0L, 64);
+  k.wp = fix(op / 9.0L, 64);
   k.wm = fix(om / 3.0L, 63);
-  k.c1 = (unsigned long long)fix(op / 2.0L, 63);
-  k.third = (unsigned long long)fix(1.0L / 3.0L, 64);
+  k.c1 = fix(op / 2.0L, 63);
+  k.third = fix(1.0L / 3.0L, 64);
   return k;
 }
 

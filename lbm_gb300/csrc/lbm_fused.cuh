@@ -96,11 +96,10 @@ __device__ __forceinline__ double bc_value(const FusedArgs& a, double s, int off
 // integer collision (collide_q60), store the 9 integers.  A cell outside the
 // range of the form stores kQ60Bad (NaN when converted back) and sets status
 // bit 0 when finite checks are on.
-__device__ __forceinline__ void bulk_cell_q60(const FusedArgs& a, long long cell) {
-  const int i = (int)(cell / a.sy);
-  const int j = (int)(cell - (long long)i * a.sy);
-  if (i == 0 || i >= a.nx - 1 || j == 0 || j >= a.ny - 1) return;
+__device__ __forceinline__ void bulk_q60_ij(const FusedArgs& a, int i, int j) {
+  if (i <= 0 || i >= a.nx - 1 || j <= 0 || j >= a.ny - 1) return;
   const long long Ns = a.Ns, sy = a.sy;
+  const long long cell = (long long)i * sy + j;
   const long long* fin = (const long long*)a.fin;
   long long x[9];
   x[0] = __ldg(fin + cell);
@@ -129,6 +128,11 @@ __device__ __forceinline__ void bulk_cell_q60(const FusedArgs& a, long long cell
   long long* fout = (long long*)a.fout;
 #pragma unroll
   for (int q = 0; q < 9; ++q) fout[q * Ns + cell] = x[q];
+}
+
+__device__ __forceinline__ void bulk_cell_q60(const FusedArgs& a, long long cell) {
+  const int i = (int)(cell / a.sy);
+  bulk_q60_ij(a, i, (int)(cell - (long long)i * a.sy));
 }
 
 template <class St, int MODE>
@@ -406,6 +410,10 @@ __device__ __forceinline__ bool on_wall_op(const FusedArgs& a, int i, int j) {
   return false;
 }
 
+template <class St>
+__device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int cell,
+                                                long long scell, CellBC<typename St::T>& c);
+
 template <class St, int MODE>
 __device__ __forceinline__ void special_cell(const FusedArgs& a, int s) {
   using S = typename St::S;
@@ -467,7 +475,56 @@ __device__ __forceinline__ void special_cell(const FusedArgs& a, int s) {
     if (si < 0 || si >= a.nx || sj < 0 || sj >= ny)
       stale_out[(long long)q * a.n_special + s] = (double)c.g[q];
   }
-  // Macro + collision in the storage form's arithmetic.
+  if constexpr (St::kFixed) {
+    // Q3.60: the post-BC populations (FP64) are converted and collided in
+    // integer arithmetic like the bulk; macro values (few cells) in FP64.
+    long long x[9];
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      x[q] = q60_from_double((double)c.g[q]);
+      ok &= x[q] != kQ60Bad;
+    }
+    const bool corner_nb = is_corner_neighbour(a, s);
+    if (corner_nb || a.write_macro) {
+      Moments<double, false> m = moments<double, false>(c.g, 0.0);
+      if (corner_nb) {
+        mac_out[s] = m.rho;
+        mac_out[a.n_special + s] = m.ux;
+        mac_out[2 * a.n_special + s] = m.uy;
+      }
+      if (a.write_macro) {
+        a.rho_out[cell] = m.rho;
+        a.u_out[cell] = m.ux;
+        a.u_out[N + cell] = m.uy;
+      }
+    }
+    long long rq, jxq, jyq;
+    ok = ok && collide_q60(x, a.kq, rq, jxq, jyq);
+    if (!ok) {
+      if (a.check_finite) atomicOr(a.status, 1u);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) x[q] = kQ60Bad;
+    }
+    long long* fout = (long long*)a.fout;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) fout[q * a.Ns + scell] = x[q];
+  } else {
+    special_collide<St>(a, s, cell, scell, c);
+  }
+}
+
+// Macro + collision of a special cell in the storage form's arithmetic.
+template <class St>
+__device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int cell,
+                                                long long scell, CellBC<typename St::T>& c) {
+  using S = typename St::S;
+  using T = typename St::T;
+  const long long N = a.N;
+  const Coef<T>& k = coef<T>(a);
+  const T rho0 = St::kShift ? T(a.kd.rho0) : T(0);
+  const long long it = *a.it_dev;
+  double* mac_out = a.mac[it & 1];
   T d[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) d[q] = St::kShift ? c.g[q] - T(wgt(q)) * rho0 : c.g[q];
