@@ -187,6 +187,15 @@ typedef struct lbm_problem {
    * for any ny.  link_cell/link_nb1/link_nb2 are indices i * row_pitch + j in
    * that layout; special_cell, g_out, rho_out and u_out use i * ny + j. */
   int32_t row_pitch;
+
+  /* Optional IBB coefficients, [3][n_links] doubles (NULL: computed from
+   * link_p in the kernel).  For link k with p = link_p[k], pp = 2p:
+   *   p <  1/2: c1 = p(pp+1), c2 = (1+pp)(1-pp), c3 = p(1-pp),
+   *             g[qb] = c1 g_up[q,x] + c2 g_up[q,x+c_qb] - c3 g_up[q,x+2c_qb]
+   *   p >= 1/2: c1 = 1/(p(pp+1)), c2 = (pp-1)/p, c3 = (1-pp)/(1+pp),
+   *             g[qb] = c1 g_up[q,x] + c2 g_up[qb,x] + c3 g_up[qb,x+c_qb]
+   * (the factors of nb.py:98-104 in the reference's evaluation order). */
+  const double* link_coef;
 } lbm_problem;
 
 /* Flags for lbm_advance. */

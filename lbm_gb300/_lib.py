@@ -66,6 +66,7 @@ class Problem(ctypes.Structure):
         ("drag_hist", _vp), ("drag_cap", _i64),
         ("rho_out", _vp), ("u_out", _vp), ("g_out", _vp), ("status_flags", _vp),
         ("row_pitch", _i32),
+        ("link_coef", _vp),
     ]
 
 

@@ -91,13 +91,41 @@ struct StoreBF16 {
 // ---------------------------------------------------------------------------
 constexpr long long kQ60Bad = (long long)0x8000000000000000ULL;
 
+// Conversions on the integer pipes (the FP64 <-> int64 conversion
+// instructions issue at the FP64 rate on GB300).  Both round to nearest,
+// ties to even, like cvt.rni.s64.f64 of v 2^60 and cvt.rn.f64.s64 of x
+// scaled by 2^-60; double -> Q3.60 is exact for |v| >= 2^-8.
 __device__ __forceinline__ long long q60_from_double(double v) {
-  if (!(fabs(v) < 8.0)) return kQ60Bad;
-  return __double2ll_rn(v * 0x1p60);
+  typedef unsigned long long ull;
+  const ull b = (ull)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e > 1025) return kQ60Bad;  // |v| >= 8, Inf or NaN
+  const ull m = (b & 0xfffffffffffffULL) | (1ULL << 52);
+  const int sh = e - 1015;  // X = m 2^(e - 1075 + 60)
+  ull X = 0;
+  if (sh >= 0) {
+    X = m << sh;
+  } else if (sh > -54) {
+    const int r = -sh;
+    const ull q = m >> r, rem = m & ((1ULL << r) - 1), half = 1ULL << (r - 1);
+    X = q + (ull)((rem > half) | ((rem == half) & (q & 1)));
+  }  // else below 2^-61: zero (zeros and subnormals included)
+  return (b >> 63) ? -(long long)X : (long long)X;
 }
 __device__ __forceinline__ double q60_to_double(long long x) {
+  typedef unsigned long long ull;
   if (x == kQ60Bad) return __longlong_as_double(0x7ff8000000000000LL);
-  return __ll2double_rn(x) * 0x1p-60;
+  if (x == 0) return 0.0;
+  const ull sgn = (ull)x & (1ULL << 63);
+  const ull a = x < 0 ? (ull)(-x) : (ull)x;
+  const int lz = __clzll((long long)a);  // >= 1
+  const ull n = a << lz;                  // leading one at bit 63
+  ull m = n >> 11;                        // 53 bits, leading one at bit 52
+  const ull rem = n & 0x7ff;
+  m += (ull)((rem > 0x400) | ((rem == 0x400) & (m & 1)));
+  // a 2^-60 has biased exponent 1026 - lz; m carries the leading one (and a
+  // rounding carry) into the exponent field.
+  return __longlong_as_double((long long)((((ull)(1025 - lz)) << 52) + m) | (long long)sgn);
 }
 
 struct StoreQ60 {
@@ -422,18 +450,42 @@ __device__ __forceinline__ void zh_corner(int corner, CellBC<T>& c, T rho_nb, T 
   c.g[0] = r - c.g[1] - c.g[2] - c.g[3] - c.g[4] - c.g[5] - c.g[6] - c.g[7] - c.g[8];
 }
 
-// Interpolated / halfway bounce-back of one link, nb.py:77-117.
-// up_q_x = g_up[q, x], up_q_1 = g_up[q, x + c_qb], up_q_2 = g_up[q, x + 2 c_qb],
-// up_qb_x = g_up[qb, x], up_qb_1 = g_up[qb, x + c_qb].
+// Interpolated bounce-back of one link, nb.py:77-117, as three coefficients
+// of the link's distance p (the parenthesised factors of the reference
+// expressions, evaluated in the same order):
+//   p <  1/2: g[qb] = c1 up_q_x + c2 up_q_1 - c3 up_q_2
+//   p >= 1/2: g[qb] = c1 up_q_x + c2 up_qb_x + c3 up_qb_1
+// with up_q_x = g_up[q, x], up_q_1 = g_up[q, x + c_qb], up_q_2 =
+// g_up[q, x + 2 c_qb], up_qb_x = g_up[qb, x], up_qb_1 = g_up[qb, x + c_qb].
+// The host computes the same coefficients once per link (link_coef).
 template <typename T>
-__device__ __forceinline__ T ibb_value(T p, T up_q_x, T up_q_1, T up_q_2, T up_qb_x, T up_qb_1) {
+__host__ __device__ __forceinline__ void ibb_coefs(T p, T& c1, T& c2, T& c3) {
   const T pp = T(2) * p;
   if (p < T(0.5)) {
-    return p * (pp + T(1)) * up_q_x + (T(1) + pp) * (T(1) - pp) * up_q_1 -
-           p * (T(1) - pp) * up_q_2;
+    c1 = p * (pp + T(1));
+    c2 = (T(1) + pp) * (T(1) - pp);
+    c3 = p * (T(1) - pp);
+  } else {
+    c1 = T(1) / (p * (pp + T(1)));
+    c2 = (pp - T(1)) / p;
+    c3 = (T(1) - pp) / (T(1) + pp);
   }
-  return (T(1) / (p * (pp + T(1)))) * up_q_x + ((pp - T(1)) / p) * up_qb_x +
-         ((T(1) - pp) / (T(1) + pp)) * up_qb_1;
+}
+
+// g[q] = v / g[q] for a run-time q in 1..8 without dynamic register indexing.
+template <typename T>
+__device__ __forceinline__ void set_pop(T g[9], int q, T v) {
+#pragma unroll
+  for (int k = 1; k < 9; ++k)
+    if (k == q) g[k] = v;
+}
+template <typename T>
+__device__ __forceinline__ T get_pop(const T g[9], int q) {
+  T v = g[0];
+#pragma unroll
+  for (int k = 1; k < 9; ++k)
+    if (k == q) v = g[k];
+  return v;
 }
 
 }  // namespace lbm

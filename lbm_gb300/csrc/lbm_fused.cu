@@ -171,6 +171,7 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.link_nb1 = p->link_nb1;
   a.link_nb2 = p->link_nb2;
   a.link_p = p->link_p;
+  a.link_coef = p->link_coef;
   a.n_links = p->n_links;
   char* base = (char*)(((uintptr_t)p->scratch + 255) & ~(uintptr_t)255);
   a.it_dev = (long long*)base;

@@ -45,6 +45,7 @@ struct FusedArgs {
   const int* link_nb1;
   const int* link_nb2;
   const double* link_p;
+  const double* link_coef;  // [3][n_links] IBB coefficients, or NULL
   // scratch: halves alternate with the parity of the iteration number
   double* stale[2];         // [9][n_special] post-BC g of an iteration
   double* mac[2];           // [3][n_special] macro rho, ux, uy of an iteration
@@ -352,22 +353,30 @@ __device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<typenam
     const int q = a.link_q[k], qb = opp(q);
     const long long x = a.link_cell[k];
     const T up_q_x = full_value<St>(fin + q * Ns + x, q, rho0);
+    T v = up_q_x;
     if (a.ibb) {
       const T p = (T)a.link_p[k];
       const long long x1 = a.link_nb1[k];
+      T c1, c2, c3;
+      if (a.link_coef) {
+        c1 = (T)a.link_coef[k];
+        c2 = (T)a.link_coef[a.n_links + k];
+        c3 = (T)a.link_coef[2 * a.n_links + k];
+      } else {
+        ibb_coefs<T>(p, c1, c2, c3);
+      }
       if (p < T(0.5)) {
         const long long x2 = a.link_nb2[k];
         const T up_q_1 = full_value<St>(fin + q * Ns + x1, q, rho0);
         const T up_q_2 = full_value<St>(fin + q * Ns + x2, q, rho0);
-        c.g[qb] = ibb_value<T>(p, up_q_x, up_q_1, up_q_2, T(0), T(0));
+        v = c1 * up_q_x + c2 * up_q_1 - c3 * up_q_2;
       } else {
         const T up_qb_x = full_value<St>(fin + qb * Ns + x, qb, rho0);
         const T up_qb_1 = full_value<St>(fin + qb * Ns + x1, qb, rho0);
-        c.g[qb] = ibb_value<T>(p, up_q_x, T(0), T(0), up_qb_x, up_qb_1);
+        v = c1 * up_q_x + c2 * up_qb_x + c3 * up_qb_1;
       }
-    } else {
-      c.g[qb] = up_q_x;
     }
+    set_pop<T>(c.g, qb, v);
   }
   // Zou-He walls in the app's order (nb.py:121-247).
   const int off_ur = 2 * ny, off_ut = 4 * ny, off_ub = 4 * ny + 2 * nx, off_rr = 4 * ny + 4 * nx;
@@ -448,7 +457,7 @@ __device__ __forceinline__ void special_cell(const FusedArgs& a, int s) {
       const int kk = a.special_link_ids[l];
       const int q = a.link_q[kk];
       const double g0 =
-          (double)full_value<St>(fin + q * a.Ns + scell, q, rho0) + (double)c.g[opp(q)];
+          (double)full_value<St>(fin + q * a.Ns + scell, q, rho0) + (double)get_pop<T>(c.g, opp(q));
       a.link_force[kk] = g0 * (double)cx(q);
       a.link_force[a.n_links + kk] = g0 * (double)cy(q);
     }

@@ -175,8 +175,23 @@ def build_tables(nx, ny, obstacles, ibb_on):
         corner_nb[c] = sp(1 if i == 0 else nx - 2, j)
     return dict(n_links=n_links, n_special=n_special, special=special, link_start=link_start,
                 link_ids=order, link_cell=link_cell, link_q=lq, nb1=nb1, nb2=nb2, p=p,
+                coef=ibb_coefficients(p),
                 obs_start=np.array(starts, np.int64), corner_special=corner_special,
                 corner_nb_special=corner_nb)
+
+
+def ibb_coefficients(p):
+    """[3][n] IBB coefficients of each link (lbm_problem.link_coef): the
+    factors of the reference's interpolated bounce-back (nb.py:98-104),
+    evaluated in its order in IEEE double."""
+    p = np.asarray(p, dtype=np.float64)
+    pp = 2.0 * p
+    lo = p < 0.5
+    with np.errstate(divide="ignore", invalid="ignore"):
+        c1 = np.where(lo, p * (pp + 1.0), 1.0 / (p * (pp + 1.0)))
+        c2 = np.where(lo, (1.0 + pp) * (1.0 - pp), (pp - 1.0) / p)
+        c3 = np.where(lo, p * (1.0 - pp), (1.0 - pp) / (1.0 + pp))
+    return np.ascontiguousarray(np.stack([c1, c2, c3]))
 
 
 class FusedEngine:
@@ -234,6 +249,7 @@ class FusedEngine:
         self.t_nb1 = i32(nb1 if n_links else np.zeros(1))
         self.t_nb2 = i32(nb2 if n_links else np.zeros(1))
         self.t_link_p = f64(p if n_links else np.zeros(1))
+        self.t_link_coef = f64(tb["coef"] if n_links else np.zeros(3))
         self.t_obs_start = i32(np.array(starts))
         self.n_links = n_links
         self.n_special = n_special
@@ -277,6 +293,7 @@ class FusedEngine:
         P.link_nb1 = self.t_nb1.data_ptr()
         P.link_nb2 = self.t_nb2.data_ptr()
         P.link_p = self.t_link_p.data_ptr()
+        P.link_coef = self.t_link_coef.data_ptr()
         P.special_link_ids = self.t_link_ids.data_ptr()
         P.n_obstacles = len(self.obstacles)
         P.obstacle_link_start = self.t_obs_start.data_ptr()
