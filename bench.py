@@ -5,20 +5,27 @@ Workload (one GPU): the large obstacle array -- ny = 2048, nx = 8192
 grid, parabolic Zou-He inlet, Zou-He pressure outlet, no-slip walls, IBB on
 every obstacle link, drag/lift of every obstacle summed every iteration.
 A "step" is one lattice iteration over all cells.  The distributions (2.4 GB
-in FP64) are far larger than the 129 MB L2, so no flush is needed between
-steps.
+in 64-bit storage) are far larger than the 129 MB L2, so no flush is needed
+between steps.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision f64]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision q60]
     python bench.py --impl reference        # CPU baseline arm (oracle port)
 
-Prints one JSON line.  ``value`` is device-timed whole-job MLUPS with the
-state resident in HBM; ``e2e`` is the same workload driven step by step
-through the host API (BC vectors uploaded from pinned host memory and the
-drag/lift of every obstacle read back every step); ``roofline`` is the bulk
-kernel's algorithmic bytes (9 loads + 9 stores per cell) over its CUDA-event
-time against the measured HBM copy bandwidth; ``cpu_baseline`` is the C
-restatement of the reference kernels (oracle/, OpenMP over all host cores)
-on a bounded sample of the same workload.
+Prints one JSON line.  ``value`` is device-timed whole-job MLUPS of the
+plain path (FP64 interface; ``q60``: 64-bit fixed-point state and integer
+bulk collision, FP64 at wall and link cells) with the state resident in HBM;
+``e2e`` is the same workload driven step by step through the host API (BC
+vectors uploaded from pinned host memory and the drag/lift of every obstacle
+read back every step); ``roofline`` is the bulk kernel's algorithmic bytes
+(9 loads + 9 stores per cell) over its CUDA-event time against the measured
+HBM copy bandwidth; ``forms`` are the other storage forms on the same
+workload (``f64``: FP64 storage and arithmetic, bounded by the FP64 pipe,
+reported with that second bound); ``form_errors`` runs the cylinder channel
+(ny 200, nx 1100, Re 100) in every form and states the error of each against
+the FP64 run; ``batched_sweep`` is the 256-case sweep; ``adjoint`` is the
+drag-gradient cost on the ny 100 channel; ``cpu_baseline`` is the C
+restatement of the reference kernels (oracle/, OpenMP over all host cores) on
+a bounded sample of the same workload.
 """
 import argparse
 import contextlib
@@ -40,6 +47,15 @@ sys.path.insert(0, ROOT)
 
 BYTES_PER_LU = {"f64": 144, "q60": 144, "f32": 72, "f16s": 36, "bf16s": 36}
 FP64_DP_OPS_PER_LU = 67  # DP instructions of the FP64 collision (lbm_device.cuh)
+ARITHMETIC = {
+    "q60": "plain path, FP64 interface: populations stored as 64-bit fixed point (Q3.60, "
+           "resolution 2^-60, exact sums), bulk collision on the integer pipes, wall and "
+           "link cells in FP64",
+    "f64": "FP64 storage and FP64 arithmetic",
+    "f32": "FP32 storage of f - w rho0, FP32 arithmetic",
+    "f16s": "FP16 storage of f - w rho0, FP32 arithmetic, FP64 drag sums",
+    "bf16s": "BF16 storage of f - w rho0, FP32 arithmetic, FP64 drag sums",
+}
 
 
 def parse():
@@ -48,10 +64,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="f64", choices=["f64", "q60", "f32", "f16s", "bf16s"])
+    ap.add_argument("--precision", default="q60", choices=["f64", "q60", "f32", "f16s", "bf16s"])
     ap.add_argument("--ny", type=int, default=2048)
-    ap.add_argument("--forms", default="f32,f16s,bf16s",
+    ap.add_argument("--forms", default="f64,f32,f16s,bf16s",
                     help="other storage forms measured in the same run ('' = none)")
+    ap.add_argument("--error-steps", type=int, default=200000,
+                    help="iterations of the cylinder-channel form-error study (0 = skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=40000,
+                    help="iterations of the adjoint cost measurement (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--sweep-steps", type=int, default=10000,
@@ -261,6 +281,164 @@ def measure_sweep(steps):
             "all_finite": True}
 
 
+def channel_app(ny, steps):
+    """Turek cylinder channel with nx = 5.5 ny (x_max = 2.055), Re 100 on the
+    cylinder diameter 0.244 ny, centred 0.49 ny from the inlet and the bottom."""
+    from lbm_gb300.apps import turek
+    a = turek()
+    a.L_lbm = ny
+    a.x_max = 2.055
+    a.compute_lbm_parameters()
+    a.stop, a.it_max, a.output_freq = "it", steps - 1, 10 ** 12
+    return a
+
+
+def run_channel(precision, ny, steps, tmp, chunk=2000):
+    """Iterations 0 .. steps-1 of the channel in one form: drag/lift series
+    (Cd, Cl of iterations 0 .. steps-2), final velocity field, MLUPS."""
+    import torch
+    import lbm_gb300
+    from lbm_gb300.engine import FusedEngine, trace_bc_program
+    app = channel_app(ny, steps)
+    with contextlib.redirect_stdout(io.StringIO()):
+        lat = lbm_gb300.lattice(app, precision=precision, output_dir=tmp, verbose=False)
+        lat.generate_image = lambda obstacles: None
+        app.initialize(lat)
+    obstacles, walls, corners = trace_bc_program(app)
+    eng = FusedEngine(lat, obstacles, walls, corners, precision=precision, drag_cap=steps + 8)
+    base, vec, scale = app.bc_schedule(lat)
+    eng.set_bc_schedule(base, vec, scale(np.arange(steps + 2)), it0=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.collide_from_g(0, macro=False)
+    it = 1
+    while it <= steps - 1:
+        n = min(chunk, steps - it)
+        eng.steps(it, n, macro_last=(it + n == steps), graph=True)
+        it += n
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    eng.check_status()
+    rows = eng.drag_rows(0, steps - 2)[:, 0, :]
+    norm = -2.0 / (app.rho_lbm * app.D_lbm * app.u_avg ** 2)
+    u = lat.device_field("u").cpu().numpy().copy()
+    del eng
+    return {"cd": rows[:, 0] * norm, "cl": rows[:, 1] * norm, "u": u,
+            "mlups": lat.nx * lat.ny * steps / dt / 1e6, "nx": lat.nx, "ny": lat.ny}
+
+
+def measure_form_errors(steps, forms, tmp, ny=200):
+    """Every form on the cylinder channel, errors stated against the FP64 run:
+    velocity-field L2 at the last iteration, and mean Cd / rms Cl / max Cd /
+    max Cl over the second half of the run."""
+    import torch
+    ref = run_channel("f64", ny, steps, tmp)
+    half = slice(len(ref["cd"]) // 2, None)
+
+    def stats(r):
+        cd, cl = r["cd"][half], r["cl"][half]
+        return {"cd_mean": float(cd.mean()), "cl_rms": float(np.sqrt((cl ** 2).mean())),
+                "cd_max": float(cd.max()), "cl_max": float(cl.max())}
+
+    sref = stats(ref)
+    out = {"case": "cylinder channel %dx%d, D = %d, Re 100, %d iterations (all forms from the "
+                   "same initial state)" % (ref["nx"], ref["ny"], channel_app(ny, 2).D_lbm, steps),
+           "f64": dict(sref, mlups=ref["mlups"])}
+    for form in forms:
+        if form == "f64":
+            continue
+        r = run_channel(form, ny, steps, tmp)
+        st = stats(r)
+        err = {k + "_rel": abs(st[k] - sref[k]) / abs(sref[k]) for k in sref}
+        err["u_l2_rel"] = float(np.linalg.norm(r["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
+        err["cd_series_max_rel"] = float(np.max(np.abs(r["cd"] - ref["cd"])) /
+                                         np.max(np.abs(ref["cd"])))
+        out[form] = dict(st, mlups=r["mlups"], error_vs_f64=err)
+        del r
+        torch.cuda.empty_cache()
+    return out
+
+
+def measure_adjoint(steps, tmp, ny=100):
+    """Gradient of the mean Cd over the last half of `steps` iterations with
+    respect to the inlet profile (every inlet row) and the TRT rate, on the
+    channel with ny = 100 (nx 550, Re 100), FP64: wall time of the gradient
+    (checkpointed forward + reverse sweep) over one plain forward run, peak
+    device memory, and a central-difference check (h = 1e-6) of dJ/d om_p and
+    of dJ/d u_in at the middle inlet row."""
+    import torch
+    import lbm_gb300
+    from lbm_gb300.adjoint import DragAdjoint, cd_weights
+    app = channel_app(ny, steps)
+    with contextlib.redirect_stdout(io.StringIO()):
+        lat = lbm_gb300.lattice(app, precision="f64", output_dir=tmp, verbose=False)
+        lat.generate_image = lambda obstacles: None
+        app.initialize(lat)
+    adj = DragAdjoint(lat, app)
+    n_obs = len(adj.eng.obstacles)
+    win = (steps - steps // 2, steps - 1)
+    w = cd_weights(app, n_obs, win[1] - win[0] + 1)
+    adj.forward(min(steps, 200), (0, 0), w, checkpoint=False)  # warm-up (graph capture)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J_plain = adj.forward(steps, win, w, checkpoint=False)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    torch.cuda.reset_peak_memory_stats()
+    base_mem = torch.cuda.memory_allocated()
+    t0 = time.perf_counter()
+    J = adj.forward(steps, win, w, checkpoint=True)
+    grad = adj.gradient()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    peak = torch.cuda.max_memory_allocated() - base_mem
+    h = 1e-6
+    om0, vec0 = lat.om_p_lbm, adj.vec.copy()
+
+    def J_at(om=om0, vec=vec0):
+        adj.set_omega(om)
+        adj.set_bc_vec(vec)
+        return adj.forward(steps, win, w, checkpoint=False)
+
+    fd_om = (J_at(om=om0 + h) - J_at(om=om0 - h)) / (2 * h)
+    j = lat.ny // 2
+    vp, vm = vec0.copy(), vec0.copy()
+    vp[j] += h
+    vm[j] -= h
+    fd_u = (J_at(vec=vp) - J_at(vec=vm)) / (2 * h)
+    J_at()
+    return {"case": "cylinder channel %dx%d, Re 100, FP64, J = mean Cd over iterations %d..%d"
+                    % (lat.nx, lat.ny, win[0], win[1]),
+            "iterations": steps, "parameters": lat.ny + 1, "J": J, "J_plain_forward": J_plain,
+            "forward_s": t_fwd, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+            "checkpoints": len(adj.ckpt), "segment": adj.K,
+            "peak_device_bytes": int(peak),
+            "fd_check": {"h": h,
+                         "omega": {"adjoint": grad["omega"], "fd": fd_om,
+                                   "rel": abs(fd_om - grad["omega"]) / abs(grad["omega"])},
+                         "u_in_row_%d" % j: {"adjoint": float(grad["bc_vec"][j]), "fd": fd_u,
+                                             "rel": abs(fd_u - grad["bc_vec"][j]) /
+                                             abs(grad["bc_vec"][j])}}}
+
+
+def fp64_bound(res):
+    """Second roofline of the FP64-arithmetic form: its DP instructions per
+    cell over the bulk kernel time, against DFMA chains timed in this run."""
+    import torch
+    from lbm_gb300 import _lib
+    L = _lib.load()
+    nbytes = L.lbm_measure_dfma_scratch_bytes()
+    buf = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    peak_dp = ctypes.c_double()
+    _lib.call("lbm_measure_dfma_rate", ctypes.byref(peak_dp), ctypes.c_void_p(buf.data_ptr()),
+              nbytes, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    rate = FP64_DP_OPS_PER_LU * res["roofline"]["units_per_launch"] / (res["kernel_ms"]["bulk"] * 1e-3)
+    return {"bound": "fp64_alu", "dp_instr_per_lu": FP64_DP_OPS_PER_LU,
+            "achieved_ginstr_s": rate / 1e9, "peak_ginstr_s": peak_dp.value,
+            "peak_source": "DFMA chains timed in this run (lbm_measure_dfma_rate)",
+            "frac": rate / 1e9 / peak_dp.value}
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (oracle port, all host threads)
 # ---------------------------------------------------------------------------
@@ -369,14 +547,30 @@ def main():
             forms[form] = {"mlups": r["mlups"], "ms_per_step": r["ms_per_step"],
                            "roofline_frac": r["roofline"]["frac"],
                            "achieved_gbs": r["roofline"]["achieved"],
-                           "kernel_ms": r["kernel_ms"],
-                           "x_vs_f64": r["mlups"] / res["mlups"]}
+                           "kernel_ms": r["kernel_ms"]}
+            if form == "f64":
+                forms[form]["second_bound"] = fp64_bound(r)
             del st
             torch.cuda.empty_cache()
+    ref64 = res["mlups"] if args.precision == "f64" else forms.get("f64", {}).get("mlups")
+    if ref64:
+        for f in forms.values():
+            f["x_vs_f64"] = f["mlups"] / ref64
+
+    form_errors = None
+    if rank == 0 and args.error_steps > 0:
+        form_errors = measure_form_errors(
+            args.error_steps, ["f64", "q60", "f32", "f16s", "bf16s"], tmp)
+        torch.cuda.empty_cache()
 
     sweep = None
     if rank == 0 and args.sweep_steps > 0:
         sweep = measure_sweep(args.sweep_steps)
+        torch.cuda.empty_cache()
+
+    adjoint = None
+    if rank == 0 and args.adjoint_steps > 0:
+        adjoint = measure_adjoint(args.adjoint_steps, tmp)
         torch.cuda.empty_cache()
 
     cpu = None
@@ -391,29 +585,19 @@ def main():
         roof["traffic"] = tr.get("bytes_per_launch")
         roof["traffic_source"] = tr.get("source")
     roof["peak_source"] = peak_src
-    second = None
-    if args.precision == "f64":
-        from lbm_gb300 import _lib
-        L = _lib.load()
-        nbytes = L.lbm_measure_dfma_scratch_bytes()
-        buf = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
-        peak_dp = ctypes.c_double()
-        _lib.call("lbm_measure_dfma_rate", ctypes.byref(peak_dp), ctypes.c_void_p(buf.data_ptr()),
-                  nbytes, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
-        rate = FP64_DP_OPS_PER_LU * res["roofline"]["units_per_launch"] / (res["kernel_ms"]["bulk"] * 1e-3)
-        second = {"bound": "fp64_alu", "dp_instr_per_lu": FP64_DP_OPS_PER_LU,
-                  "achieved_ginstr_s": rate / 1e9, "peak_ginstr_s": peak_dp.value,
-                  "peak_source": "DFMA chains timed in this run (lbm_measure_dfma_rate)",
-                  "frac": rate / 1e9 / peak_dp.value}
+    dtype = {"q60": "int64", "f64": "f64", "f32": "f32", "f16s": "f16", "bf16s": "bf16"}
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": args.precision, "data": "synthetic", "config": cfg,
-        "roofline": roof, "second_bound": second,
+        "dtype": dtype[args.precision], "form": args.precision,
+        "arithmetic": ARITHMETIC[args.precision],
+        "data": "synthetic", "config": cfg,
+        "roofline": roof, "second_bound": fp64_bound(res) if args.precision == "f64" else None,
         "kernel_ms": res["kernel_ms"], "e2e": e2e,
-        "gpu_launches": args.steps * res["kernels_per_step"] + 1,
-        "clocks": clocks, "forms": forms, "batched_sweep": sweep, "cpu_baseline": cpu,
+        "gpu_launches": args.steps * res["kernels_per_step"],
+        "clocks": clocks, "forms": forms, "form_errors": form_errors,
+        "batched_sweep": sweep, "adjoint": adjoint, "cpu_baseline": cpu,
     }
     if rank == 0:
         print(json.dumps(line))

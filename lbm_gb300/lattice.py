@@ -96,6 +96,14 @@ def _mirror_property(name):
     return property(getter, setter)
 
 
+def default_precision(rho0, om_p, om_m):
+    """The plain path's default form: "q60" (64-bit fixed-point state, integer
+    bulk collision; at least FP64's resolution for populations above 2^-7)
+    when the case is inside its range, else "f64"."""
+    ok = 0.75 <= rho0 <= 1.5 and all(1.0 / 1024 <= om <= 1.999 for om in (om_p, om_m))
+    return "q60" if ok else "f64"
+
+
 class lattice:
     """Device-resident D2Q9 TRT lattice with the reference lattice API."""
 
@@ -141,9 +149,9 @@ class lattice:
         if hasattr(app, "Cr"):
             self.Cr = app.Ct  # the reference copies Ct into Cr (lattice.py:63)
 
-        # Storage form of the fused engine ("f64" is the plain path).
-        self.precision = precision or getattr(app, "precision", "f64")
-        if self.precision not in _lib.PRECISIONS:
+        # Storage form of the fused engine, checked once the TRT rates are set.
+        self.precision = precision or getattr(app, "precision", None)
+        if self.precision is not None and self.precision not in _lib.PRECISIONS:
             raise ValueError("precision must be one of %s" % sorted(_lib.PRECISIONS))
 
         # Output directories (lattice.py:80-91).
@@ -162,6 +170,8 @@ class lattice:
         if self.device.index is None:
             self.device = torch.device("cuda", torch.cuda.current_device())
         self.set_default_lbm()
+        if self.precision is None:
+            self.precision = default_precision(self.rho_lbm, self.om_p_lbm, self.om_m_lbm)
         self._obs_cache = {}
         self._replay = None
         self._drag_scratch = None
