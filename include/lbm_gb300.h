@@ -293,6 +293,22 @@ size_t lbm_adjoint_omega_slots(const lbm_problem* p);
  * dJ/dx_prev given lam_in = dJ/d g_up(it).  FP64 arrays, reference layout. */
 int lbm_adjoint_step(const lbm_problem* p, const lbm_adjoint* adj, int64_t it,
                      const double* x_prev, const double* lam_in, double* lam_out, void* stream);
+/* Recompute one checkpoint segment: with states[0] (FP64, reference layout)
+ * = x(it_first), write x(it_first + m) into states + m * stride for
+ * m = 1 .. n_steps - 1 (forward steps without drag history).  stride >=
+ * 9 * nx * ny elements.  Uses the problem's scratch: one recompute at a time
+ * per problem; it may run on another stream than lbm_adjoint_sweep, which
+ * does not touch the scratch.  No counterpart in the reference. */
+int lbm_adjoint_recompute(const lbm_problem* p, int64_t it_first, int n_steps, double* states,
+                          int64_t stride, void* stream);
+/* Reverse sweep over a recomputed segment: lbm_adjoint_step for it =
+ * it_first + n_steps down to it_first + 1 with x_prev = states + (it - 1 -
+ * it_first) * stride and lambda ping-ponging between lam0/lam1: lam[parity]
+ * holds dJ/dx(it_first + n_steps) on entry and lam[parity ^ (n_steps & 1)]
+ * holds dJ/dx(it_first) on return.  No counterpart in the reference. */
+int lbm_adjoint_sweep(const lbm_problem* p, const lbm_adjoint* adj, int64_t it_first,
+                      int n_steps, const double* states, int64_t stride, double* lam0,
+                      double* lam1, int parity, void* stream);
 /* First collision (from the initial g0): adds its om_p term, lam_out = dJ/dg0. */
 int lbm_adjoint_initial(const lbm_problem* p, const lbm_adjoint* adj, const double* g0,
                         const double* lam_in, double* lam_out, void* stream);

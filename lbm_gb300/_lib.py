@@ -126,6 +126,10 @@ _SIGS = {
     "lbm_adjoint_omega_slots": ([ctypes.POINTER(Problem)], ctypes.c_size_t),
     "lbm_adjoint_step": ([ctypes.POINTER(Problem), ctypes.POINTER(Adjoint), _i64, _vp, _vp, _vp,
                           _vp], ctypes.c_int),
+    "lbm_adjoint_recompute": ([ctypes.POINTER(Problem), _i64, ctypes.c_int, _vp, _i64, _vp],
+                              ctypes.c_int),
+    "lbm_adjoint_sweep": ([ctypes.POINTER(Problem), ctypes.POINTER(Adjoint), _i64, ctypes.c_int,
+                           _vp, _i64, _vp, _vp, ctypes.c_int, _vp], ctypes.c_int),
     "lbm_adjoint_initial": ([ctypes.POINTER(Problem), ctypes.POINTER(Adjoint), _vp, _vp, _vp,
                              _vp], ctypes.c_int),
     "lbm_pack_f64": ([ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _vp],

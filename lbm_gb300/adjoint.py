@@ -8,14 +8,15 @@ set_bc must give every wall a Zou-He operation and apply the four corners).
   K = ceil(sqrt(T)) iterations; returns J = sum over the window of
   sum_o (w_fx[o] fx_o + w_fy[o] fy_o), fx/fy the raw drag/lift sums.
 * ``gradient()``: sweeps the segments from the last to the first; each
-  segment is recomputed from its checkpoint into a K-slot buffer and then
-  walked backwards with ``lbm_adjoint_step``; returns dJ/d om_p, dJ/d(BC
-  vector entries) scaled like the BC schedule (``bc_vec``: entry k of the
-  packed u_left | u_right | u_top | u_bot | rho_right vectors, value(it) =
-  base + scale(it) vec) and dJ/d(base).
+  segment is recomputed from its checkpoint into a K-slot buffer
+  (``lbm_adjoint_recompute``, on a second stream, one segment ahead of the
+  sweep) and then walked backwards (``lbm_adjoint_sweep``); returns
+  dJ/d om_p, dJ/d(BC vector entries) scaled like the BC schedule
+  (``bc_vec``: entry k of the packed u_left | u_right | u_top | u_bot |
+  rho_right vectors, value(it) = base + scale(it) vec) and dJ/d(base).
 
-Memory: T/K checkpoints + K recomputed states + two adjoint states, i.e.
-about 2 sqrt(T) copies of the lattice instead of T.
+Memory: T/K checkpoints + 2 K recomputed states + two adjoint states, i.e.
+about 3 sqrt(T) copies of the lattice instead of T.
 """
 import ctypes
 import math
@@ -132,24 +133,47 @@ class DragAdjoint:
         A.grad_omega_len = slots
         lam = [torch.zeros(9 * N, dtype=torch.float64, device=dev) for _ in range(2)]
         cur = 0  # lam[cur] = lambda(n)
-        seg_buf = torch.empty((self.K, 9 * N), dtype=torch.float64, device=dev)
+        # Two segment buffers: the segment before the one being swept back is
+        # recomputed meanwhile on a second stream (the sweep's kernels are
+        # latency-bound and leave the GPU room).
+        seg_bufs = [torch.empty((self.K, 9 * N), dtype=torch.float64, device=dev)
+                    for _ in range(2)]
         starts = sorted(self.ckpt)
-        st = self._stream()
-        for s0 in reversed(starts):
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        ready = [torch.cuda.Event(), torch.cuda.Event()]
+        free = [torch.cuda.Event(), torch.cuda.Event()]
+
+        def recompute(k, b):
+            s0 = starts[k]
             s1 = min(s0 + self.K, self.T)
-            # recompute x(s0) .. x(s1 - 1) into seg_buf
-            eng.f[0].copy_(self.ckpt[s0])
-            eng.cur = 0
-            seg_buf[0].copy_(eng.f[0].reshape(-1))
-            for m in range(1, s1 - s0):
-                eng.steps(s0 + m, 1, graph=False)
-                seg_buf[m].copy_(eng.f[eng.cur].reshape(-1))
-            for n in range(s1, s0, -1):
-                x_prev = seg_buf[n - 1 - s0]
-                _lib.call("lbm_adjoint_step", ctypes.byref(eng.P), ctypes.byref(A), n,
-                          ctypes.c_void_p(x_prev.data_ptr()), ctypes.c_void_p(lam[cur].data_ptr()),
-                          ctypes.c_void_p(lam[cur ^ 1].data_ptr()), st)
-                cur ^= 1
+            side.wait_event(free[b])
+            with torch.cuda.stream(side):
+                seg_bufs[b][0].copy_(self.ckpt[s0].reshape(-1))
+                _lib.call("lbm_adjoint_recompute", ctypes.byref(eng.P), s0, s1 - s0,
+                          ctypes.c_void_p(seg_bufs[b].data_ptr()), 9 * N,
+                          ctypes.c_void_p(side.cuda_stream))
+            ready[b].record(side)
+
+        for b in range(2):
+            free[b].record(main)
+        order = list(range(len(starts)))[::-1]
+        recompute(order[0], 0)
+        for n, k in enumerate(order):
+            b = n & 1
+            if n + 1 < len(order):
+                recompute(order[n + 1], b ^ 1)
+            s0 = starts[k]
+            s1 = min(s0 + self.K, self.T)
+            main.wait_event(ready[b])
+            # walk back s1 .. s0 + 1 over x(s0) .. x(s1 - 1)
+            _lib.call("lbm_adjoint_sweep", ctypes.byref(eng.P), ctypes.byref(A), s0, s1 - s0,
+                      ctypes.c_void_p(seg_bufs[b].data_ptr()), 9 * N,
+                      ctypes.c_void_p(lam[0].data_ptr()), ctypes.c_void_p(lam[1].data_ptr()),
+                      cur, ctypes.c_void_p(main.cuda_stream))
+            free[b].record(main)
+            cur ^= (s1 - s0) & 1
+        st = self._stream()
         # the first collision x(0) = collide(g0)
         _lib.call("lbm_adjoint_initial", ctypes.byref(eng.P), ctypes.byref(A),
                   ctypes.c_void_p(self.g0.data_ptr()), ctypes.c_void_p(lam[cur].data_ptr()),

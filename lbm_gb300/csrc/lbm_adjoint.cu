@@ -9,19 +9,23 @@
 // om_p (om_m follows from om_p, lattice.py:127-131) and to every entry of the
 // packed BC vectors of iteration n-1:
 //
-//   k_adj_bulk     every non-wall cell: recompute the pulled values, apply
-//                  the transposed collision Jacobian (hand-derived: linear
-//                  pair part plus a rank-3 update through rho, jx, jy),
-//                  store the adjoint of each pulled value; d/d om_p terms.
-//   k_adj_corners  the four corner cells: reverse their chain (corner op,
-//                  walls, links); the corner op reads rho/u of the
-//                  x-neighbour, whose adjoint seeds are handed on.
-//   k_adj_special  every other special cell: collision transposed, drag
-//                  seeds, then the chain reversed op by op.  The BC ops are
-//                  small, so each op's transposed Jacobian is taken with
-//                  forward-mode dual numbers (one pass per input) on the
-//                  same templated code the forward uses; the IBB rows are
-//                  written out by hand.
+//   k_adj_cells    one launch over every cell:
+//                  - bulk cells (one per thread): recompute the pulled
+//                    values, apply the transposed collision Jacobian
+//                    (hand-derived: linear pair part plus a rank-3 update
+//                    through rho, jx, jy), store the adjoint of each pulled
+//                    value; d/d om_p terms;
+//                  - special cells other than corners (one per warp):
+//                    collision transposed, drag seeds, then the chain
+//                    reversed op by op.  The BC ops are small, so each op's
+//                    transposed Jacobian is taken with forward-mode dual
+//                    numbers, one Jacobian column per lane, on the same
+//                    templated code the forward uses; the IBB rows are
+//                    written out by hand;
+//                  - the four corners (one per warp): their chain reversed
+//                    (corner op, walls, links).  The corner op reads rho/u of
+//                    the x-neighbour; the neighbour's warp recomputes that
+//                    seed itself, so no cell waits for another.
 //   k_adj_gather   lambda(n-1)[q, y] = adjoint of the value pulled by cell
 //                  y + c_q (the transpose of the pull).
 //   k_adj_links    add the IBB and drag terms that read x(n-1) directly.
@@ -96,15 +100,19 @@ __device__ __forceinline__ void apply_wall(int op, CellBC<T>& c, T p0, T p1) {
   }
 }
 
-// Transposed Jacobian-vector product of a BC op by forward-mode columns.
-// in: state before the op; adj: adjoint of the state after it (replaced by
-// the adjoint of the state before it); params/adj_params: np op parameters.
-// kind < 5: wall op `kind`; kind 5 + c: corner c with params (rho, ux, uy)
-// of the x-neighbour.
+// Transposed Jacobian-vector product of a BC op by forward-mode columns,
+// warp-cooperative: every lane of the warp calls it with the same arguments;
+// lane k < 12 + np propagates the derivative with respect to input k (one
+// Jacobian column), and the column-adjoint dot products are exchanged by
+// shuffles.  in: state before the op; adj: adjoint of the state after it
+// (replaced by the adjoint of the state before it); params/adj_params: np op
+// parameters.  kind < 5: wall op `kind`; kind 5 + c: corner c with params
+// (rho, ux, uy) of the x-neighbour.
 __device__ void op_transpose(int kind, const CellBC<double>& in, const double* params, int np,
                              CellBC<double>& adj, double* adj_params) {
-  double res[15];
-  for (int k = 0; k < 12 + np; ++k) {
+  const int k = threadIdx.x & 31;
+  double s = 0.0;
+  if (k < 12 + np) {
     CellBC<Dual> c;
 #pragma unroll
     for (int q = 0; q < 9; ++q) c.g[q] = Dual(in.g[q], k == q ? 1.0 : 0.0);
@@ -118,17 +126,19 @@ __device__ void op_transpose(int kind, const CellBC<double>& in, const double* p
     } else {
       zh_corner<Dual>(kind - 5, c, p[0], p[1], p[2]);
     }
-    double s = c.rho.d * adj.rho + c.ux.d * adj.ux + c.uy.d * adj.uy;
+    s = c.rho.d * adj.rho + c.ux.d * adj.ux + c.uy.d * adj.uy;
 #pragma unroll
     for (int q = 0; q < 9; ++q) s += c.g[q].d * adj.g[q];
-    res[k] = s;
   }
 #pragma unroll
-  for (int q = 0; q < 9; ++q) adj.g[q] = res[q];
-  adj.rho = res[9];
-  adj.ux = res[10];
-  adj.uy = res[11];
-  for (int m = 0; m < np; ++m) adj_params[m] = res[12 + m];
+  for (int q = 0; q < 9; ++q) adj.g[q] = __shfl_sync(0xffffffffu, s, q);
+  adj.rho = __shfl_sync(0xffffffffu, s, 9);
+  adj.ux = __shfl_sync(0xffffffffu, s, 10);
+  adj.uy = __shfl_sync(0xffffffffu, s, 11);
+  for (int m = 0; m < 3; ++m) {
+    const double v = __shfl_sync(0xffffffffu, s, 12 + m);
+    if (m < np) adj_params[m] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -242,7 +252,6 @@ struct AdjArgs {
   double* grad_bc_base;
   double* grad_bc_vec;
   double* grad_omega;     // per-block partial sums
-  int omega_special_off, omega_corner_off;
   const unsigned char* is_special;  // [N]
   const double* obj_w;    // [2][n_obs] weights of fx, fy
   int in_window;          // the drag of iteration it-1 enters the objective
@@ -260,36 +269,31 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_adj_bulk(AdjArgs A) {
-  __shared__ double sh[256];
+// Bulk cell: transposed collision of the pulled values (one thread per cell).
+__device__ __forceinline__ double adj_bulk_cell(const AdjArgs& A, long long cell) {
   const FusedArgs& a = A.f;
   const long long N = a.N;
-  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double dom = 0.0;
-  if (cell < N) {
-    const int i = (int)(cell / a.ny), j = (int)(cell - (long long)i * a.ny);
-    if (i > 0 && i < a.nx - 1 && j > 0 && j < a.ny - 1 && !A.is_special[cell]) {
-      const double* x = (const double*)a.fin;
-      const long long ny = a.ny;
-      double d[9], lam[9], adj[9];
-      d[0] = x[cell];
-      d[1] = x[1 * N + cell - ny];
-      d[2] = x[2 * N + cell + ny];
-      d[3] = x[3 * N + cell - 1];
-      d[4] = x[4 * N + cell + 1];
-      d[5] = x[5 * N + cell - ny - 1];
-      d[6] = x[6 * N + cell + ny + 1];
-      d[7] = x[7 * N + cell + ny - 1];
-      d[8] = x[8 * N + cell - ny + 1];
+  if (cell >= N) return 0.0;
+  const int i = (int)(cell / a.ny), j = (int)(cell - (long long)i * a.ny);
+  if (i <= 0 || i >= a.nx - 1 || j <= 0 || j >= a.ny - 1 || A.is_special[cell]) return 0.0;
+  const double* x = (const double*)a.fin;
+  const long long ny = a.ny;
+  double d[9], lam[9], adj[9];
+  d[0] = x[cell];
+  d[1] = x[1 * N + cell - ny];
+  d[2] = x[2 * N + cell + ny];
+  d[3] = x[3 * N + cell - 1];
+  d[4] = x[4 * N + cell + 1];
+  d[5] = x[5 * N + cell - ny - 1];
+  d[6] = x[6 * N + cell + ny + 1];
+  d[7] = x[7 * N + cell + ny - 1];
+  d[8] = x[8 * N + cell - ny + 1];
 #pragma unroll
-      for (int q = 0; q < 9; ++q) lam[q] = A.lam_in[q * N + cell];
-      dom = collide_transpose(d, lam, A.k, adj);
+  for (int q = 0; q < 9; ++q) lam[q] = A.lam_in[q * N + cell];
+  const double dom = collide_transpose(d, lam, A.k, adj);
 #pragma unroll
-      for (int q = 0; q < 9; ++q) A.adj_pulled[q * N + cell] = adj[q];
-    }
-  }
-  const double s = block_sum(dom, sh);
-  if (threadIdx.x == 0) A.grad_omega[blockIdx.x] += s;
+  for (int q = 0; q < 9; ++q) A.adj_pulled[q * N + cell] = adj[q];
+  return dom;
 }
 
 // Op list of special cell s: links [0, nl), wall ops touching the cell, then
@@ -381,7 +385,7 @@ __device__ void chain_prefix(const AdjArgs& A, int s, int i, int j, const OpList
     double coef[3], v[3];
     link_rows(a, k, coef);
     link_reads(a, k, v);
-    c.g[opp(a.link_q[k])] = coef[0] * v[0] + coef[1] * v[1] + coef[2] * v[2];
+    set_pop<double>(c.g, opp(a.link_q[k]), coef[0] * v[0] + coef[1] * v[1] + coef[2] * v[2]);
   }
   for (int w = 0; w < o.nw && op < K; ++w, ++op) {
     double p[2];
@@ -390,49 +394,76 @@ __device__ void chain_prefix(const AdjArgs& A, int s, int i, int j, const OpList
   }
 }
 
+// Pulled/link state, the state before each of the first two wall ops and the
+// state after all wall ops (corner excluded) of special cell s, in one pass.
+__device__ void chain_states(const AdjArgs& A, int s, int i, int j, const OpList& o,
+                             CellBC<double> pre_wall[2], CellBC<double>& c) {
+  chain_prefix(A, s, i, j, o, o.nl, c);
+  for (int w = 0; w < o.nw; ++w) {
+    if (w < 2) pre_wall[w] = c;
+    double p[2];
+    wall_params(A, o.walls[w], i, j, p);
+    apply_wall<double>(o.walls[w], c, p[0], p[1]);
+  }
+}
+
 // Reverse the non-corner part of the chain: adj (adjoint after the last
 // wall op) -> adjoint of the pulled values; link reads and BC gradients are
-// emitted.
+// emitted.  pre_wall: states before the first two wall ops (chain_states).
+// Warp-cooperative (one warp per cell, lane 0 writes).
 __device__ void reverse_chain(const AdjArgs& A, int s, int i, int j, const OpList& o,
-                              CellBC<double>& adj) {
+                              const CellBC<double> pre_wall[2], CellBC<double>& adj) {
   const FusedArgs& a = A.f;
+  const bool lead = (threadIdx.x & 31) == 0;  // the warp's writer
   for (int w = o.nw - 1; w >= 0; --w) {
     CellBC<double> c;
-    chain_prefix(A, s, i, j, o, o.nl + w, c);
+    if (w < 2) {
+      c = pre_wall[w];
+    } else {
+      chain_prefix(A, s, i, j, o, o.nl + w, c);
+    }
     double p[2], ap[2];
     wall_params(A, o.walls[w], i, j, p);
     op_transpose(o.walls[w], c, p, 2, adj, ap);
     int k0, k1;
     wall_param_index(o.walls[w], i, j, a.nx, a.ny, k0, k1);
-    A.grad_bc_base[k0] += ap[0];
-    A.grad_bc_base[k1] += ap[1];
     const double bs = bc_scale_at(a, A.it - 1);
-    A.grad_bc_vec[k0] += bs * ap[0];
-    A.grad_bc_vec[k1] += bs * ap[1];
+    if (lead) {
+      A.grad_bc_base[k0] += ap[0];
+      A.grad_bc_base[k1] += ap[1];
+      A.grad_bc_vec[k0] += bs * ap[0];
+      A.grad_bc_vec[k1] += bs * ap[1];
+    }
   }
   for (int l = o.nl - 1; l >= 0; --l) {
     const int k = a.special_link_ids[o.l0 + l];
     const int qb = opp(a.link_q[k]);
     double coef[3];
     link_rows(a, k, coef);
-    const double ag = adj.g[qb];
-    A.link_adj[k] += coef[0] * ag;
-    A.link_adj[a.n_links + k] += coef[1] * ag;
-    A.link_adj[2 * a.n_links + k] += coef[2] * ag;
-    adj.g[qb] = 0.0;  // overwritten by the link
+    const double ag = get_pop<double>(adj.g, qb);
+    if (lead) {
+      A.link_adj[k] += coef[0] * ag;
+      A.link_adj[a.n_links + k] += coef[1] * ag;
+      A.link_adj[2 * a.n_links + k] += coef[2] * ag;
+    }
+    set_pop<double>(adj.g, qb, 0.0);  // overwritten by the link
   }
   const long long cell = (long long)i * a.ny + j;
+  if (lead) {
 #pragma unroll
-  for (int q = 0; q < 9; ++q) {
-    const int si = i - cx(q), sj = j - cy(q);
-    const bool pulled = si >= 0 && si < a.nx && sj >= 0 && sj < a.ny;
-    A.adj_pulled[q * a.N + cell] = pulled ? adj.g[q] : 0.0;
+    for (int q = 0; q < 9; ++q) {
+      const int si = i - cx(q), sj = j - cy(q);
+      const bool pulled = si >= 0 && si < a.nx && sj >= 0 && sj < a.ny;
+      A.adj_pulled[q * a.N + cell] = pulled ? adj.g[q] : 0.0;
+    }
   }
 }
 
-// Collision transpose + drag seeds of special cell s, given its post-BC g.
+// Collision transpose + drag seeds of special cell s, given its post-BC g
+// (warp-cooperative; the om_p term is returned by lane 0 only).
 __device__ double seed_special(const AdjArgs& A, int s, long long cell, const OpList& o,
-                               const CellBC<double>& post, CellBC<double>& adj) {
+                               const CellBC<double>& post, CellBC<double>& adj,
+                               bool write = true) {
   const FusedArgs& a = A.f;
   double lam[9], ad[9];
 #pragma unroll
@@ -442,99 +473,124 @@ __device__ double seed_special(const AdjArgs& A, int s, long long cell, const Op
   for (int q = 0; q < 9; ++q) adj.g[q] = ad[q];
   adj.rho = adj.ux = adj.uy = 0.0;
   // drag/lift of iteration it - 1: (x(n-1)[q, x] + g_post[qb, x]) c_q per link
+  const bool lead = (threadIdx.x & 31) == 0;
   for (int l = 0; l < o.nl; ++l) {
     const int k = a.special_link_ids[o.l0 + l];
-    A.link_adj[k] = 0.0;
-    A.link_adj[a.n_links + k] = 0.0;
-    A.link_adj[2 * a.n_links + k] = 0.0;
-  }
-  if (A.in_window) {
-    for (int l = 0; l < o.nl; ++l) {
-      const int k = a.special_link_ids[o.l0 + l];
+    double wgt_k = 0.0;
+    if (A.in_window) {
       const int q = a.link_q[k];
       int ob = 0;  // obstacle of link k
       while (ob + 1 < a.n_obs && a.obs_start[ob + 1] <= k) ++ob;
-      const double wgt_k = A.obj_w[ob] * (double)cx(q) + A.obj_w[a.n_obs + ob] * (double)cy(q);
-      adj.g[opp(q)] += wgt_k;
-      A.link_adj[k] += wgt_k;  // the x(n-1)[q, x] term
+      wgt_k = A.obj_w[ob] * (double)cx(q) + A.obj_w[a.n_obs + ob] * (double)cy(q);
+      set_pop<double>(adj.g, opp(q), get_pop<double>(adj.g, opp(q)) + wgt_k);
+    }
+    if (lead && write) {
+      A.link_adj[k] = wgt_k;  // the x(n-1)[q, x] term
+      A.link_adj[a.n_links + k] = 0.0;
+      A.link_adj[2 * a.n_links + k] = 0.0;
     }
   }
+  return lead ? dom : 0.0;
+}
+
+// Adjoint of corner op cn: the corner cell's collision transpose and drag
+// seeds, then the corner op transposed.  Returns in adj the adjoint of the
+// corner's state before the corner op (with its pre-wall states and op list
+// for reverse_chain) and in ap the adjoint of the x-neighbour's (rho, ux,
+// uy) that the corner op reads (nb.py:254-257).  write = false computes the
+// same values without writing the corner's link terms (the neighbour's warp
+// recomputes the seed it needs instead of waiting for the corner's warp).
+__device__ double corner_adjoint(const AdjArgs& A, int cn, bool write, CellBC<double>& adj,
+                                 double ap[3], CellBC<double> pre_wall[2], OpList& o) {
+  const FusedArgs& a = A.f;
+  const int s = a.corner_special[cn];
+  const int cell = a.special_cell[s];
+  const int i = cell / a.ny, j = cell - i * a.ny;
+  o = op_list(a, s, i, j);
+  // neighbour state after its own links and walls
+  const int snb = a.corner_nb_special[cn];
+  const int cnb = a.special_cell[snb];
+  const int inb = cnb / a.ny, jnb = cnb - inb * a.ny;
+  const OpList onb = op_list(a, snb, inb, jnb);
+  CellBC<double> nb;
+  chain_prefix(A, snb, inb, jnb, onb, onb.nl + onb.nw, nb);
+  const double params[3] = {nb.rho, nb.ux, nb.uy};
+  CellBC<double> pre, post;
+  chain_states(A, s, i, j, o, pre_wall, pre);
+  post = pre;
+  zh_corner<double>(cn, post, params[0], params[1], params[2]);
+  const double dom = seed_special(A, s, cell, o, post, adj, write);
+  op_transpose(5 + cn, pre, params, 3, adj, ap);
   return dom;
 }
 
-__global__ void __launch_bounds__(128) k_adj_special(AdjArgs A) {
-  __shared__ double sh[128];
+// Special cell s that is not a corner (warp-cooperative).
+__device__ double adj_special_cell(const AdjArgs& A, int s) {
   const FusedArgs& a = A.f;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double dom = 0.0;
-  if (s < a.n_special) {
-    const int cell = a.special_cell[s];
-    const int i = cell / a.ny, j = cell - i * a.ny;
-    const OpList o = op_list(a, s, i, j);
-    if (o.corner < 0) {
-      CellBC<double> post, adj;
-      chain_prefix(A, s, i, j, o, o.nl + o.nw, post);
-      dom = seed_special(A, s, cell, o, post, adj);
-      // corner seeds for an x-neighbour of a corner: adjoint of its rho/u
-      for (int w = 0; w < a.n_corner_ops; ++w) {
-        const int cn = a.corner_ops[w];
-        if (a.corner_nb_special[cn] == s) {
-          adj.rho += A.corner_seed[3 * cn];
-          adj.ux += A.corner_seed[3 * cn + 1];
-          adj.uy += A.corner_seed[3 * cn + 2];
-        }
-      }
-      reverse_chain(A, s, i, j, o, adj);
+  const int cell = a.special_cell[s];
+  const int i = cell / a.ny, j = cell - i * a.ny;
+  const OpList o = op_list(a, s, i, j);
+  if (o.corner >= 0) return 0.0;
+  CellBC<double> pre_wall[2], post, adj;
+  chain_states(A, s, i, j, o, pre_wall, post);
+  const double dom = seed_special(A, s, cell, o, post, adj);
+  // x-neighbour of a corner: add the adjoint of the rho/u the corner read
+  for (int w = 0; w < a.n_corner_ops; ++w) {
+    const int cn = a.corner_ops[w];
+    if (a.corner_nb_special[cn] == s) {
+      CellBC<double> cadj, cpre[2];
+      OpList co;
+      double ap[3];
+      corner_adjoint(A, cn, false, cadj, ap, cpre, co);
+      adj.rho += ap[0];
+      adj.ux += ap[1];
+      adj.uy += ap[2];
     }
   }
-  const double t = block_sum(dom, sh);
-  if (threadIdx.x == 0) A.grad_omega[A.omega_special_off + blockIdx.x] += t;
+  reverse_chain(A, s, i, j, o, pre_wall, adj);
+  return dom;
 }
 
-// One thread per corner op (launched before k_adj_special, which reads the seeds).
-__global__ void k_adj_corners(AdjArgs A) {
+// Corner op number w of the program (warp-cooperative).
+__device__ double adj_corner(const AdjArgs& A, int w) {
   const FusedArgs& a = A.f;
-  const int w = threadIdx.x;
+  const int cn = a.corner_ops[w];
+  CellBC<double> adj, pre_wall[2];
+  OpList o;
+  double ap[3];
+  const double dom = corner_adjoint(A, cn, true, adj, ap, pre_wall, o);
+  const int s = a.corner_special[cn];
+  const int cell = a.special_cell[s];
+  const int i = cell / a.ny, j = cell - i * a.ny;
+  reverse_chain(A, s, i, j, o, pre_wall, adj);
+  return dom;
+}
+
+// Every cell of the adjoint step in one launch (128 threads per block):
+// blocks [0, nbb) bulk cells, one per thread; blocks [nbb, nbb + nbs) special
+// cells other than corners, one per warp; the last block the corner ops,
+// one per warp.  Corner chains, special cells and bulk cells run side by
+// side.  Each block adds its part of d/d om_p to grad_omega[block].
+__global__ void __launch_bounds__(128) k_adj_cells(AdjArgs A, int nbb, int nbs) {
+  __shared__ double sh[128];
+  const FusedArgs& a = A.f;
   double dom = 0.0;
-  if (w < a.n_corner_ops) {
-    const int cn = a.corner_ops[w];
-    const int s = a.corner_special[cn];
-    const int cell = a.special_cell[s];
-    const int i = cell / a.ny, j = cell - i * a.ny;
-    const OpList o = op_list(a, s, i, j);
-    // neighbour state after its own links and walls
-    const int snb = a.corner_nb_special[cn];
-    const int cnb = a.special_cell[snb];
-    const int inb = cnb / a.ny, jnb = cnb - inb * a.ny;
-    const OpList onb = op_list(a, snb, inb, jnb);
-    CellBC<double> nb;
-    chain_prefix(A, snb, inb, jnb, onb, onb.nl + onb.nw, nb);
-    const double params[3] = {nb.rho, nb.ux, nb.uy};
-    CellBC<double> pre, post;
-    chain_prefix(A, s, i, j, o, o.nl + o.nw, pre);
-    post = pre;
-    zh_corner<double>(cn, post, params[0], params[1], params[2]);
-    CellBC<double> adj;
-    dom = seed_special(A, s, cell, o, post, adj);
-    double ap[3];
-    op_transpose(5 + cn, pre, params, 3, adj, ap);
-    A.corner_seed[3 * cn] = ap[0];
-    A.corner_seed[3 * cn + 1] = ap[1];
-    A.corner_seed[3 * cn + 2] = ap[2];
-    reverse_chain(A, s, i, j, o, adj);
+  const int b = blockIdx.x;
+  if (b < nbb) {
+    dom = adj_bulk_cell(A, (long long)b * blockDim.x + threadIdx.x);
+  } else if (b < nbb + nbs) {
+    const int s = (b - nbb) * 4 + (int)(threadIdx.x >> 5);
+    if (s < a.n_special) dom = adj_special_cell(A, s);
+  } else {
+    const int w = threadIdx.x >> 5;
+    if (w < a.n_corner_ops) dom = adj_corner(A, w);
   }
-  __shared__ double part[4];
-  if (w < 4) part[w] = dom;
-  __syncthreads();
-  if (w == 0) {
-    double t = 0.0;
-    for (int m = 0; m < 4 && m < (int)blockDim.x; ++m) t += part[m];
-    A.grad_omega[A.omega_corner_off] += t;
-  }
+  const double t = block_sum(dom, sh);
+  if (threadIdx.x == 0) A.grad_omega[b] += t;
 }
 
 // lambda(n-1)[q, y] = adjoint of the value pulled by cell y + c_q.
-__global__ void __launch_bounds__(256) k_adj_gather(AdjArgs A) {
+__global__ void __launch_bounds__(128) k_adj_gather(AdjArgs A) {
   const FusedArgs& a = A.f;
   const long long N = a.N;
   const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -615,23 +671,35 @@ using namespace lbm;
 extern "C" size_t lbm_adjoint_omega_slots(const lbm_problem* p) {
   if (!p) return 0;
   const long long N = (long long)p->nx * p->ny;
-  return (size_t)((N + 255) / 256 + (p->n_special + 127) / 128 + 1);
+  return (size_t)((N + 127) / 128 + (p->n_special + 3) / 4 + 1);
 }
 
-extern "C" int lbm_adjoint_step(const lbm_problem* p, const lbm_adjoint* adj, int64_t it,
-                                const double* x_prev, const double* lam_in, double* lam_out,
-                                void* stream) {
-  if (int rc = problem_check(p, "lbm_adjoint_step")) return rc;
+namespace {
+int adjoint_args_check(const lbm_problem* p, const lbm_adjoint* adj, const char* fn) {
+  if (int rc = problem_check(p, fn)) return rc;
   if (!adjoint_supported(p)) {
-    set_error("lbm_adjoint_step: needs FP64, a Zou-He operation on every wall and all four "
-              "corners");
+    set_error("%s: needs FP64, a Zou-He operation on every wall and all four corners", fn);
     return LBM_ERR_UNSUPPORTED;
   }
-  if (!adj || !x_prev || !lam_in || !lam_out || !adj->adj_pulled || !adj->grad_bc_base ||
-      !adj->grad_bc_vec || !adj->grad_omega || !adj->is_special || !adj->corner_seed ||
-      (p->n_links > 0 && !adj->link_adj) || (p->n_obstacles > 0 && !adj->obj_w) || it < 1 ||
+  if (!adj || !adj->adj_pulled || !adj->grad_bc_base || !adj->grad_bc_vec || !adj->grad_omega ||
+      !adj->is_special || !adj->corner_seed || (p->n_links > 0 && !adj->link_adj) ||
+      (p->n_obstacles > 0 && !adj->obj_w) ||
       (size_t)adj->grad_omega_len < lbm_adjoint_omega_slots(p)) {
-    set_error("lbm_adjoint_step: bad arguments");
+    set_error("%s: bad arguments", fn);
+    return LBM_ERR_ARG;
+  }
+  return LBM_OK;
+}
+
+// Enqueue adjoint step `it` (checked arguments).
+int adjoint_enqueue(const lbm_problem* p, const lbm_adjoint* adj, int64_t it, const double* x_prev,
+                    const double* lam_in, double* lam_out, cudaStream_t st, const char* fn) {
+  if (!x_prev || !lam_in || !lam_out || it < 1) {
+    set_error("%s: bad arguments", fn);
+    return LBM_ERR_ARG;
+  }
+  if (p->bc_vec && ((it - 1) - p->bc_scale_it0 < 0 || (it - 1) - p->bc_scale_it0 >= p->bc_scale_len)) {
+    set_error("%s: BC scale table does not cover iteration %lld", fn, (long long)it - 1);
     return LBM_ERR_ARG;
   }
   AdjArgs A;
@@ -648,25 +716,74 @@ extern "C" int lbm_adjoint_step(const lbm_problem* p, const lbm_adjoint* adj, in
   A.grad_bc_vec = adj->grad_bc_vec;
   A.grad_omega = adj->grad_omega;
   const long long N = (long long)p->nx * p->ny;
-  const int nb_bulk = (int)((N + 255) / 256);
-  const int nb_special = (p->n_special + 127) / 128;
-  A.omega_special_off = nb_bulk;
-  A.omega_corner_off = nb_bulk + nb_special;
+  const int nbb = (int)((N + 127) / 128);
+  const int nbs = (p->n_special + 3) / 4;  // one warp per special cell
   A.is_special = adj->is_special;
   A.obj_w = adj->obj_w;
   A.it = it;
   A.in_window = (it - 1 >= adj->obj_it_first && it - 1 <= adj->obj_it_last) ? 1 : 0;
-  if (p->bc_vec && ((it - 1) - p->bc_scale_it0 < 0 || (it - 1) - p->bc_scale_it0 >= p->bc_scale_len)) {
-    set_error("lbm_adjoint_step: BC scale table does not cover iteration %lld", (long long)it - 1);
+  k_adj_cells<<<nbb + nbs + 1, 128, 0, st>>>(A, nbb, nbs);
+  k_adj_gather<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(A);
+  if (p->n_links > 0) k_adj_links<<<(p->n_links + 255) / 256, 256, 0, st>>>(A);
+  LBM_CUDA_CHECK(cudaGetLastError(), fn);
+  return LBM_OK;
+}
+}  // namespace
+
+extern "C" int lbm_adjoint_step(const lbm_problem* p, const lbm_adjoint* adj, int64_t it,
+                                const double* x_prev, const double* lam_in, double* lam_out,
+                                void* stream) {
+  if (int rc = adjoint_args_check(p, adj, "lbm_adjoint_step")) return rc;
+  return adjoint_enqueue(p, adj, it, x_prev, lam_in, lam_out, (cudaStream_t)stream,
+                         "lbm_adjoint_step");
+}
+
+extern "C" int lbm_adjoint_recompute(const lbm_problem* p, int64_t it_first, int n_steps,
+                                     double* states, int64_t stride, void* stream) {
+  const char* fn = "lbm_adjoint_recompute";
+  if (int rc = problem_check(p, fn)) return rc;
+  if (!adjoint_supported(p)) {
+    set_error("%s: needs FP64, a Zou-He operation on every wall and all four corners", fn);
+    return LBM_ERR_UNSUPPORTED;
+  }
+  const long long N9 = 9LL * p->nx * p->ny;
+  if (!states || n_steps < 1 || it_first < 0 || stride < N9) {
+    set_error("%s: bad arguments", fn);
     return LBM_ERR_ARG;
   }
+  // Each step reads one slot and writes the next; no drag history (the
+  // objective is known from the forward run).
+  lbm_problem q = *p;
+  q.drag_hist = nullptr;
   cudaStream_t st = (cudaStream_t)stream;
-  k_adj_bulk<<<nb_bulk, 256, 0, st>>>(A);
-  k_adj_corners<<<1, 4, 0, st>>>(A);
-  k_adj_special<<<nb_special, 128, 0, st>>>(A);
-  k_adj_gather<<<nb_bulk, 256, 0, st>>>(A);
-  if (p->n_links > 0) k_adj_links<<<(p->n_links + 255) / 256, 256, 0, st>>>(A);
-  LBM_CUDA_CHECK(cudaGetLastError(), "lbm_adjoint_step");
+  for (int m = 1; m < n_steps; ++m) {
+    q.f[0] = states + (m - 1) * stride;
+    q.f[1] = states + m * stride;
+    if (int rc = fused_enqueue(&q, LBM_MODE_STEP, it_first + m, 1, 0, 0, m == 1, st)) return rc;
+  }
+  return LBM_OK;
+}
+
+extern "C" int lbm_adjoint_sweep(const lbm_problem* p, const lbm_adjoint* adj, int64_t it_first,
+                                 int n_steps, const double* states, int64_t stride, double* lam0,
+                                 double* lam1, int parity, void* stream) {
+  const char* fn = "lbm_adjoint_sweep";
+  if (int rc = adjoint_args_check(p, adj, fn)) return rc;
+  const long long N9 = 9LL * p->nx * p->ny;
+  if (!states || !lam0 || !lam1 || n_steps < 1 || it_first < 0 || stride < N9 ||
+      (parity != 0 && parity != 1)) {
+    set_error("%s: bad arguments", fn);
+    return LBM_ERR_ARG;
+  }
+  double* lam[2] = {lam0, lam1};
+  int cur = parity;
+  for (int64_t n = it_first + n_steps; n > it_first; --n) {
+    const double* x_prev = states + (n - 1 - it_first) * stride;
+    if (int rc = adjoint_enqueue(p, adj, n, x_prev, lam[cur], lam[cur ^ 1], (cudaStream_t)stream,
+                                 fn))
+      return rc;
+    cur ^= 1;
+  }
   return LBM_OK;
 }
 
