@@ -259,7 +259,7 @@ extern "C" int lbm_advance_graph(const lbm_problem* p, int64_t it0, int n_steps,
     hit = &g_cache.back();
   }
   hit->last_use = ++g_clock;
-  if (int rc = fused_set_it(p, it0 - 1, st)) return rc;
+  if (int rc = fused_set_it(p, it0, st)) return rc;
   LBM_CUDA_CHECK(cudaGraphLaunch(hit->exec, st), "lbm_advance_graph: launch");
   return LBM_OK;
 }

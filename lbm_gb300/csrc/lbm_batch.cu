@@ -46,12 +46,10 @@ namespace {
 template <class St>
 __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict__ args,
                                                     const int4* __restrict__ tiles, int n_tiles,
-                                                    unsigned* queue, long long* it_dev) {
+                                                    unsigned* queue, long long* it_dev, int last) {
   constexpr int V = 16 / (int)sizeof(typename St::S);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *it_dev += 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
     queue[1] = 0;  // the special phase of this iteration starts from tile 0
-  }
   __shared__ int t_sh;
   for (;;) {
     if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[0], 1u);
@@ -69,6 +67,7 @@ __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict_
         bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
     }
   }
+  if (last) advance_counter(it_dev, queue + 2);
 }
 
 // Same work as k_batch_bulk with one block per tile (the hardware block
@@ -76,12 +75,10 @@ __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict_
 template <class St>
 __global__ void __launch_bounds__(256) k_batch_bulk_grid(const FusedArgs* __restrict__ args,
                                                          const int4* __restrict__ tiles,
-                                                         unsigned* queue, long long* it_dev) {
+                                                         unsigned* queue, long long* it_dev,
+                                                         int last) {
   constexpr int V = 16 / (int)sizeof(typename St::S);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *it_dev += 1;
-    queue[1] = 0;
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) queue[1] = 0;
   const int4 tl = tiles[blockIdx.x];
   const FusedArgs& a = args[tl.x];
   if (tl.w) {
@@ -90,21 +87,25 @@ __global__ void __launch_bounds__(256) k_batch_bulk_grid(const FusedArgs* __rest
     for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
       bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
   }
+  if (last) advance_counter(it_dev, queue + 2);
 }
 
 template <class St>
 __global__ void __launch_bounds__(128) k_batch_special_grid(const FusedArgs* __restrict__ args,
                                                             const int4* __restrict__ tiles,
-                                                            unsigned* queue) {
+                                                            unsigned* queue, long long* it_dev,
+                                                            int last) {
   if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;
   const int4 tl = tiles[blockIdx.x];
   if ((int)threadIdx.x < tl.z) special_cell<St, LBM_MODE_STEP>(args[tl.x], tl.y + threadIdx.x);
+  if (last) advance_counter(it_dev, queue + 2);
 }
 
 template <class St>
 __global__ void __launch_bounds__(128) k_batch_special(const FusedArgs* __restrict__ args,
                                                        const int4* __restrict__ tiles, int n_tiles,
-                                                       unsigned* queue) {
+                                                       unsigned* queue, long long* it_dev,
+                                                       int last) {
   if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;  // next iteration's bulk queue
   __shared__ int t_sh;
   for (;;) {
@@ -117,36 +118,45 @@ __global__ void __launch_bounds__(128) k_batch_special(const FusedArgs* __restri
     for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
       special_cell<St, LBM_MODE_STEP>(args[tl.x], tl.y + k);
   }
+  if (last) advance_counter(it_dev, queue + 2);
 }
 
 __global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict__ args,
-                                                    const int2* __restrict__ items, int n_items) {
-  if ((int)blockIdx.x >= n_items) return;
-  const int2 it = items[blockIdx.x];
-  drag_obstacle(args[it.x], it.y);
+                                                    const int2* __restrict__ items, int n_items,
+                                                    unsigned* queue, long long* it_dev) {
+  if ((int)blockIdx.x < n_items) {
+    const int2 it = items[blockIdx.x];
+    drag_obstacle(args[it.x], it.y);
+  }
+  advance_counter(it_dev, queue + 2);  // the drag kernel is always last
 }
 
 template <class St>
 void enqueue_store(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
   const int gb = b->sm_count * b->cfg.bulk_blocks_per_sm;
   const int gs = b->sm_count * b->cfg.special_blocks_per_sm;
+  // The step's last kernel advances the shared iteration counter.
+  const bool drag = b->n_drag_items > 0, special = b->n_special_tiles > 0;
+  const int bulk_last = !drag && !special, special_last = !drag && special;
   for (int k = 0; k < n_steps; ++k) {
     const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
     if (b->cfg.persistent) {
       k_batch_bulk<St><<<gb, b->cfg.bulk_threads, 0, st>>>(args, b->d_bulk_tiles,
-                                                           b->n_bulk_tiles, b->d_queue, b->d_it);
-      if (b->n_special_tiles > 0)
+                                                           b->n_bulk_tiles, b->d_queue, b->d_it,
+                                                           bulk_last);
+      if (special)
         k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
-                                                b->d_queue);
+                                                b->d_queue, b->d_it, special_last);
     } else {
       k_batch_bulk_grid<St><<<b->n_bulk_tiles, b->cfg.bulk_threads, 0, st>>>(
-          args, b->d_bulk_tiles, b->d_queue, b->d_it);
-      if (b->n_special_tiles > 0)
-        k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(args, b->d_special_tiles,
-                                                                     b->d_queue);
+          args, b->d_bulk_tiles, b->d_queue, b->d_it, bulk_last);
+      if (special)
+        k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(
+            args, b->d_special_tiles, b->d_queue, b->d_it, special_last);
     }
-    if (b->n_drag_items > 0)
-      k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items);
+    if (drag)
+      k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items,
+                                                    b->d_queue, b->d_it);
   }
 }
 
@@ -166,10 +176,12 @@ int batch_enqueue(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) 
   return LBM_OK;
 }
 
+// queue[0]: bulk tile queue, [1]: special tile queue, [2]: step-done count.
 __global__ void k_batch_set_it(long long* it, long long v, unsigned* queue) {
   *it = v;
   queue[0] = 0;
   queue[1] = 0;
+  queue[2] = 0;
 }
 
 void batch_free(lbm_batch* b) {
@@ -231,7 +243,7 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       FusedArgs a = make_args(&p, LBM_MODE_STEP, LBM_FLAG_CHECK_FINITE);
       a.fin = p.f[par];
       a.fout = p.f[par ^ 1];
-      a.advance_it = 0;
+      a.advance_at = -1;  // the batch kernels advance the shared counter
       a.write_macro = 0;
       args[(size_t)par * n_cases + c] = a;
     }
@@ -280,7 +292,10 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
     return LBM_ERR_CUDA;
   }
   // Every lattice reads the shared counter.
-  for (auto& a : args) a.it_dev = b->d_it;
+  for (auto& a : args) {
+    a.it_dev = b->d_it;
+    a.step_done = b->d_queue + 2;
+  }
   e = cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(FusedArgs), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     set_error("lbm_batch_create: %s", cudaGetErrorString(e));
@@ -314,7 +329,7 @@ extern "C" int lbm_batch_advance(lbm_batch* b, int64_t it0, int n_steps, int par
     return LBM_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  k_batch_set_it<<<1, 1, 0, st>>>(b->d_it, it0 - 1, b->d_queue);
+  k_batch_set_it<<<1, 1, 0, st>>>(b->d_it, it0, b->d_queue);
   return batch_enqueue(b, n_steps, parity, st);
 }
 
@@ -355,7 +370,7 @@ extern "C" int lbm_batch_advance_graph(lbm_batch* b, int64_t it0, int n_steps, i
     b->g_parity.push_back(parity);
     b->g_exec.push_back(exec);
   }
-  k_batch_set_it<<<1, 1, 0, st>>>(b->d_it, it0 - 1, b->d_queue);
+  k_batch_set_it<<<1, 1, 0, st>>>(b->d_it, it0, b->d_queue);
   LBM_CUDA_CHECK(cudaGetLastError(), "lbm_batch_advance_graph");
   LBM_CUDA_CHECK(cudaGraphLaunch(exec, st), "lbm_batch_advance_graph: launch");
   return LBM_OK;

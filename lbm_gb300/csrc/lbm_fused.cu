@@ -27,16 +27,15 @@ namespace lbm {
 template <class St, int MODE>
 __global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
   const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell == 0 && a.advance_it) *a.it_dev += 1;
-  if (cell >= a.Ns) return;
-  bulk_cell<St, MODE>(a, cell);
+  if (cell < a.Ns) bulk_cell<St, MODE>(a, cell);
+  if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
 template <class St, int V>
 __global__ void __launch_bounds__(128) k_bulk_vec(FusedArgs a) {
   const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi == 0 && a.advance_it) *a.it_dev += 1;
   bulk_group_vec<St, V>(a, gi);
+  if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
 // Q3.60 bulk kernel: block b covers column i = b / jb, rows
@@ -44,23 +43,26 @@ __global__ void __launch_bounds__(128) k_bulk_vec(FusedArgs a) {
 __global__ void __launch_bounds__(256) k_bulk_q60(FusedArgs a, int jb) {
   const int i = blockIdx.x / jb;
   const int j = (blockIdx.x - i * jb) * 256 + threadIdx.x;
-  if (blockIdx.x == 0 && threadIdx.x == 0 && a.advance_it) *a.it_dev += 1;
   bulk_q60_ij(a, i, j);
+  if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
 template <class St, int MODE>
 __global__ void __launch_bounds__(128) k_special(FusedArgs a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.n_special) return;
-  special_cell<St, MODE>(a, s);
+  if (s < a.n_special) special_cell<St, MODE>(a, s);
+  if (a.advance_at == 1) advance_counter(a.it_dev, a.step_done);
 }
 
 __global__ void __launch_bounds__(256) k_drag(FusedArgs a) {
-  if ((int)blockIdx.x >= a.n_obs) return;
-  drag_obstacle(a, blockIdx.x);
+  if ((int)blockIdx.x < a.n_obs) drag_obstacle(a, blockIdx.x);
+  if (a.advance_at == 2) advance_counter(a.it_dev, a.step_done);
 }
 
-__global__ void k_set_it(long long* it_dev, long long value) { *it_dev = value; }
+__global__ void k_set_it(long long* it_dev, unsigned* done, long long value) {
+  *it_dev = value;
+  *done = 0;
+}
 
 // ---------------------------------------------------------------------------
 // Host side
@@ -68,7 +70,11 @@ __global__ void k_set_it(long long* it_dev, long long value) { *it_dev = value; 
 // ev (optional): four events recorded before k_bulk, k_special, k_drag and
 // after the step, for per-kernel timing.
 template <class St, int MODE>
-static void launch_mode(const FusedArgs& a, cudaStream_t st, cudaEvent_t* ev) {
+static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
+  FusedArgs a = a0;
+  const bool with_special = a.n_special > 0;
+  const bool with_drag = MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0;
+  a.advance_at = with_drag ? 2 : (with_special ? 1 : 0);
   const int tb = 256;
   const long long nb = (a.Ns + tb - 1) / tb;
   // 16-byte vectors for the reduced storage forms (8 FP16/BF16 or 4 FP32 cells).
@@ -85,13 +91,12 @@ static void launch_mode(const FusedArgs& a, cudaStream_t st, cudaEvent_t* ev) {
     k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[1], st);
-  if (a.n_special > 0) {
+  if (with_special) {
     const int ts = 128;
     k_special<St, MODE><<<(a.n_special + ts - 1) / ts, ts, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[2], st);
-  if (MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0)
-    k_drag<<<a.n_obs, 256, 0, st>>>(a);
+  if (with_drag) k_drag<<<a.n_obs, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
 }
 
@@ -110,7 +115,8 @@ int fused_kernels_per_step(const lbm_problem* p, int mode) {
   return n;
 }
 
-// Scratch layout: iteration counter (256 B) | stale[2][9][n_special] |
+// Scratch layout: iteration counter and step-done count (256 B) |
+// stale[2][9][n_special] |
 // mac[2][3][n_special] | link_force[2][n_links]   (doubles).
 size_t fused_scratch_bytes(const lbm_problem* p) {
   size_t ns = (size_t)(p->n_special > 0 ? p->n_special : 0);
@@ -175,6 +181,7 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.n_links = p->n_links;
   char* base = (char*)(((uintptr_t)p->scratch + 255) & ~(uintptr_t)255);
   a.it_dev = (long long*)base;
+  a.step_done = (unsigned*)(base + 8);
   double* sc = (double*)(base + 256);
   const size_t ns = (size_t)p->n_special;
   a.stale[0] = sc;
@@ -191,18 +198,18 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.g_out = p->g_out;
   a.status = p->status_flags;
   a.mode = mode;
-  a.advance_it = 1;
+  a.advance_at = 0;
   a.check_finite = (flags & LBM_FLAG_CHECK_FINITE) && p->status_flags ? 1 : 0;
   a.wall_macro = (flags & LBM_FLAG_WALL_MACRO) && p->rho_out && p->u_out ? 1 : 0;
   return a;
 }
 
-// Enqueue n_steps steps.  set_it: write it0 - 1 into the device counter first
+// Enqueue n_steps steps.  set_it: write it0 into the device counter first
 // (left out when a graph that must not bake the start iteration is captured).
 int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, int parity,
                   unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev) {
   FusedArgs a = make_args(p, mode, flags);
-  if (set_it) k_set_it<<<1, 1, 0, st>>>(a.it_dev, it0 - 1);
+  if (set_it) k_set_it<<<1, 1, 0, st>>>(a.it_dev, a.step_done, it0);
   for (int k = 0; k < n_steps; ++k) {
     const int par = (parity + k) & 1;  // f[par] holds g_up of the previous iteration
     a.fin = p->f[par];
@@ -227,7 +234,7 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
 
 int fused_set_it(const lbm_problem* p, long long value, cudaStream_t st) {
   char* base = (char*)(((uintptr_t)p->scratch + 255) & ~(uintptr_t)255);
-  k_set_it<<<1, 1, 0, st>>>((long long*)base, value);
+  k_set_it<<<1, 1, 0, st>>>((long long*)base, (unsigned*)(base + 8), value);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("lbm_advance: launch failed: %s", cudaGetErrorString(e));

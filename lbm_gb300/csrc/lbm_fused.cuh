@@ -31,10 +31,12 @@ struct FusedArgs {
   const double* bc_scale;
   long long bc_scale_it0, bc_scale_len;
   // Device iteration counter: the iteration whose collision the running step
-  // does.  k_bulk (first kernel of a step) advances it, so a captured graph
-  // replays correctly from any starting iteration.
+  // does.  The step's last kernel advances it when its last block finishes
+  // (advance_counter), so every kernel of a step reads the same value and a
+  // captured graph replays correctly from any starting iteration.
   long long* it_dev;
-  int advance_it;
+  unsigned* step_done;  // blocks of the last kernel that have finished
+  int advance_at;       // kernel that advances: 0 bulk, 1 special, 2 drag, -1 none
   // special cells / links
   int n_special;
   const int* special_cell;
@@ -66,6 +68,22 @@ struct FusedArgs {
   int wall_macro;
   int check_finite;
 };
+
+// Called by every block of a step's last kernel after its work: the last
+// block to arrive advances the iteration counter.  Every block has read the
+// counter before it arrives; no block waits for another.
+__device__ __forceinline__ void advance_counter(long long* it_dev, unsigned* done) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned n = gridDim.x * gridDim.y * gridDim.z;
+    if (atomicAdd(done, 1u) == n - 1) {
+      *done = 0;
+      *it_dev += 1;
+      __threadfence();
+    }
+  }
+}
 
 template <typename T>
 __device__ __forceinline__ const Coef<T>& coef(const FusedArgs& a);
