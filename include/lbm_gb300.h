@@ -252,6 +252,8 @@ typedef struct lbm_batch_config {
   int32_t scalar_tile_cells;     /* cells per tile of lattices without 16-byte rows */
   int32_t persistent;            /* 1: persistent blocks pull tiles from an atomic
                                     queue; 0: one block per tile                  */
+  int32_t vec_bytes;             /* 8 or 16: bytes per vector access of the bulk
+                                    kernel (cells per thread = this / element)    */
 } lbm_batch_config;
 int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32_t n_cases,
                      const lbm_batch_config* cfg);

@@ -9,8 +9,10 @@
   advances all of them with ``lbm_batch_advance_graph``: per iteration one
   persistent bulk kernel over a tile work queue of every lattice, one
   persistent special-cell kernel and one drag kernel.
-* ``autotune(batch)``  picks threads per block, persistent grid size and the
-  number of iterations per CUDA graph by timing candidates on the batch.
+* ``autotune(batch)``  picks the scheduling (persistent work queue or one
+  block per tile), the vector width of the bulk kernel (cells per thread),
+  threads per block, persistent grid size and the number of iterations per
+  CUDA graph by timing candidates on the batch.
 """
 import contextlib
 import ctypes
@@ -152,7 +154,7 @@ class Batch:
         arr = (_lib.Problem * len(self.engines))(*[e.P for e in self.engines])
         c = _lib.BatchConfig(cfg["bulk_threads"], cfg["bulk_blocks_per_sm"],
                              cfg["special_blocks_per_sm"], cfg["scalar_tile_cells"],
-                             int(cfg.get("persistent", 1)))
+                             int(cfg.get("persistent", 1)), int(cfg.get("vec_bytes", 16)))
         h = ctypes.c_void_p()
         _lib.call("lbm_batch_create", ctypes.byref(h), arr, len(self.engines), ctypes.byref(c))
         self.handle = h
@@ -192,7 +194,7 @@ class Batch:
 
 def default_config():
     return {"bulk_threads": 128, "bulk_blocks_per_sm": 8, "special_blocks_per_sm": 8,
-            "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 1}
+            "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 1, "vec_bytes": 16}
 
 
 def time_batch(batch, n_steps, k=None):
@@ -216,6 +218,7 @@ def autotune(batch, steps=60, space=None, verbose=False):
     """
     space = space or {
         "persistent": [1, 0],
+        "vec_bytes": [16, 8],
         "bulk_threads": [64, 128, 256],
         "bulk_blocks_per_sm": [4, 8],
         "special_blocks_per_sm": [8],

@@ -43,11 +43,15 @@ struct lbm_batch {
 namespace lbm {
 namespace {
 
-template <class St>
+
+// VB: bytes per vector access (a group of VB / sizeof(element) cells per
+// thread; lbm_batch_config.vec_bytes).  kVecOnly: every tile is a vector
+// tile (no scalar path compiled in).
+template <class St, int VB, bool kVecOnly>
 __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict__ args,
                                                     const int4* __restrict__ tiles, int n_tiles,
                                                     unsigned* queue, long long* it_dev, int last) {
-  constexpr int V = 16 / (int)sizeof(typename St::S);
+  constexpr int V = VB / (int)sizeof(typename St::S);
   if (blockIdx.x == 0 && threadIdx.x == 0)
     queue[1] = 0;  // the special phase of this iteration starts from tile 0
   __shared__ int t_sh;
@@ -60,9 +64,9 @@ __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict_
     const int4 tl = tiles[t];
     const FusedArgs& a = args[tl.x];
     if (tl.w) {
-      // one 16-byte group per thread; tiles are blockDim groups long
+      // one vector group per thread; tiles are blockDim groups long
       bulk_group_vec<St, V>(a, (long long)tl.y + threadIdx.x);
-    } else {
+    } else if (!kVecOnly) {
       for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
         bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
     }
@@ -72,18 +76,18 @@ __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict_
 
 // Same work as k_batch_bulk with one block per tile (the hardware block
 // scheduler distributes the tiles; no queue).
-template <class St>
+template <class St, int VB, bool kVecOnly>
 __global__ void __launch_bounds__(256) k_batch_bulk_grid(const FusedArgs* __restrict__ args,
                                                          const int4* __restrict__ tiles,
                                                          unsigned* queue, long long* it_dev,
                                                          int last) {
-  constexpr int V = 16 / (int)sizeof(typename St::S);
+  constexpr int V = VB / (int)sizeof(typename St::S);
   if (blockIdx.x == 0 && threadIdx.x == 0) queue[1] = 0;
   const int4 tl = tiles[blockIdx.x];
   const FusedArgs& a = args[tl.x];
   if (tl.w) {
     bulk_group_vec<St, V>(a, (long long)tl.y + threadIdx.x);
-  } else {
+  } else if (!kVecOnly) {
     for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
       bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
   }
@@ -131,8 +135,8 @@ __global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict_
   advance_counter(it_dev, queue + 2);  // the drag kernel is always last
 }
 
-template <class St>
-void enqueue_store(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
+template <class St, int VB, bool kVecOnly>
+void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
   const int gb = b->sm_count * b->cfg.bulk_blocks_per_sm;
   const int gs = b->sm_count * b->cfg.special_blocks_per_sm;
   // The step's last kernel advances the shared iteration counter.
@@ -141,14 +145,13 @@ void enqueue_store(const lbm_batch* b, int n_steps, int parity, cudaStream_t st)
   for (int k = 0; k < n_steps; ++k) {
     const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
     if (b->cfg.persistent) {
-      k_batch_bulk<St><<<gb, b->cfg.bulk_threads, 0, st>>>(args, b->d_bulk_tiles,
-                                                           b->n_bulk_tiles, b->d_queue, b->d_it,
-                                                           bulk_last);
+      k_batch_bulk<St, VB, kVecOnly><<<gb, b->cfg.bulk_threads, 0, st>>>(
+          args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
       if (special)
         k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
                                                 b->d_queue, b->d_it, special_last);
     } else {
-      k_batch_bulk_grid<St><<<b->n_bulk_tiles, b->cfg.bulk_threads, 0, st>>>(
+      k_batch_bulk_grid<St, VB, kVecOnly><<<b->n_bulk_tiles, b->cfg.bulk_threads, 0, st>>>(
           args, b->d_bulk_tiles, b->d_queue, b->d_it, bulk_last);
       if (special)
         k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(
@@ -157,6 +160,17 @@ void enqueue_store(const lbm_batch* b, int n_steps, int parity, cudaStream_t st)
     if (drag)
       k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items,
                                                     b->d_queue, b->d_it);
+  }
+}
+
+template <class St>
+void enqueue_store(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
+  if (b->cfg.vec_bytes == 8) {
+    if (b->any_scalar) enqueue_store_vb<St, 8, false>(b, n_steps, parity, st);
+    else enqueue_store_vb<St, 8, true>(b, n_steps, parity, st);
+  } else {
+    if (b->any_scalar) enqueue_store_vb<St, 16, false>(b, n_steps, parity, st);
+    else enqueue_store_vb<St, 16, true>(b, n_steps, parity, st);
   }
 }
 
@@ -212,7 +226,8 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       cfg->bulk_blocks_per_sm < 1 || cfg->bulk_blocks_per_sm > 32 ||
       cfg->special_blocks_per_sm < 1 || cfg->special_blocks_per_sm > 32 ||
       cfg->scalar_tile_cells < 32 || cfg->scalar_tile_cells > (1 << 20) ||
-      (cfg->persistent != 0 && cfg->persistent != 1)) {
+      (cfg->persistent != 0 && cfg->persistent != 1) ||
+      (cfg->vec_bytes != 8 && cfg->vec_bytes != 16)) {
     set_error("lbm_batch_create: bad config (threads %d, blocks/SM %d/%d, tile %d)",
               cfg->bulk_threads, cfg->bulk_blocks_per_sm, cfg->special_blocks_per_sm,
               cfg->scalar_tile_cells);
@@ -226,7 +241,9 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       return LBM_ERR_ARG;
     }
   }
-  const int V = (prec == LBM_PREC_F64 || prec == LBM_PREC_Q60) ? 1 : (prec == LBM_PREC_F32 ? 4 : 8);
+  const int V = (prec == LBM_PREC_F64 || prec == LBM_PREC_Q60)
+                    ? 1
+                    : cfg->vec_bytes / (prec == LBM_PREC_F32 ? 4 : 2);
   std::vector<FusedArgs> args(2 * (size_t)n_cases);
   std::vector<int4> bulk, special;
   std::vector<int2> drag;
@@ -269,6 +286,8 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  b->any_scalar = 0;
+  for (const int4& t : bulk) b->any_scalar |= t.w == 0;
   b->n_bulk_tiles = (int)bulk.size();
   b->n_special_tiles = (int)special.size();
   b->n_drag_items = (int)drag.size();
