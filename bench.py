@@ -45,7 +45,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_LU = {"f64": 144, "q60": 144, "f32": 72, "f16s": 36, "bf16s": 36}
+BYTES_PER_LU = {"f64": 144, "q60": 144, "f32": 72, "f16s": 36, "bf16s": 36, "f16sr": 36,
+                "bf16sr": 36}
+FORMS = ["f64", "q60", "f32", "f16s", "f16sr", "bf16s", "bf16sr"]
 FP64_DP_OPS_PER_LU = 67  # DP instructions of the FP64 collision (lbm_device.cuh)
 ARITHMETIC = {
     "q60": "plain path, FP64 interface: populations stored as 64-bit fixed point (Q3.60, "
@@ -55,6 +57,10 @@ ARITHMETIC = {
     "f32": "FP32 storage of f - w rho0, FP32 arithmetic",
     "f16s": "FP16 storage of f - w rho0, FP32 arithmetic, FP64 drag sums",
     "bf16s": "BF16 storage of f - w rho0, FP32 arithmetic, FP64 drag sums",
+    "f16sr": "FP16 storage of f - w rho0 with stochastic rounding, FP32 arithmetic, FP64 drag "
+             "sums",
+    "bf16sr": "BF16 storage of f - w rho0 with stochastic rounding, FP32 arithmetic, FP64 drag "
+              "sums",
 }
 
 
@@ -64,9 +70,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="q60", choices=["f64", "q60", "f32", "f16s", "bf16s"])
+    ap.add_argument("--precision", default="q60", choices=FORMS)
     ap.add_argument("--ny", type=int, default=2048)
-    ap.add_argument("--forms", default="f64,f32,f16s,bf16s",
+    ap.add_argument("--forms", default="f64,f32,f16s,f16sr,bf16s,bf16sr",
                     help="other storage forms measured in the same run ('' = none)")
     ap.add_argument("--error-steps", type=int, default=200000,
                     help="iterations of the cylinder-channel form-error study (0 = skip)")
@@ -562,8 +568,7 @@ def main():
 
     form_errors = None
     if rank == 0 and args.error_steps > 0:
-        form_errors = measure_form_errors(
-            args.error_steps, ["f64", "q60", "f32", "f16s", "bf16s"], tmp)
+        form_errors = measure_form_errors(args.error_steps, FORMS, tmp)
         torch.cuda.empty_cache()
 
     sweep = None
@@ -588,7 +593,8 @@ def main():
         roof["traffic"] = tr.get("bytes_per_launch")
         roof["traffic_source"] = tr.get("source")
     roof["peak_source"] = peak_src
-    dtype = {"q60": "int64", "f64": "f64", "f32": "f32", "f16s": "f16", "bf16s": "bf16"}
+    dtype = {"q60": "int64", "f64": "f64", "f32": "f32", "f16s": "f16", "bf16s": "bf16",
+             "f16sr": "f16", "bf16sr": "bf16"}
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,

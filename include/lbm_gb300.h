@@ -46,6 +46,11 @@ extern "C" {
  * INT64_MIN, which unpacks to NaN.  No counterpart in the reference (its FP64
  * path computes in FP64). */
 #define LBM_PREC_Q60 4
+/* FP16 / BF16 storage of f - w*rho0 as LBM_PREC_F16S / LBM_PREC_BF16S, with
+ * stochastic rounding of every update (deterministic: the random bits hash
+ * the cell and the iteration).  No counterpart in the reference. */
+#define LBM_PREC_F16SR 5
+#define LBM_PREC_BF16SR 6
 
 /* Wall operations (Zou-He), lbm/src/core/nb.py:121-247. */
 #define LBM_WALL_LEFT_VELOCITY 0

@@ -16,9 +16,9 @@ LBM_ERR_CUDA = 2
 LBM_ERR_NONFINITE = 3
 LBM_ERR_UNSUPPORTED = 5
 
-PREC_F64, PREC_F32, PREC_F16S, PREC_BF16S, PREC_Q60 = 0, 1, 2, 3, 4
+PREC_F64, PREC_F32, PREC_F16S, PREC_BF16S, PREC_Q60, PREC_F16SR, PREC_BF16SR = range(7)
 PRECISIONS = {"f64": PREC_F64, "f32": PREC_F32, "f16s": PREC_F16S, "bf16s": PREC_BF16S,
-              "q60": PREC_Q60}
+              "q60": PREC_Q60, "f16sr": PREC_F16SR, "bf16sr": PREC_BF16SR}
 
 WALL_LEFT_VELOCITY = 0
 WALL_RIGHT_VELOCITY = 1

@@ -27,7 +27,7 @@ int problem_check(const lbm_problem* p, const char* fn) {
     set_error("%s: lattice %d x %d outside 4 <= n, nx*ny < 2^31", fn, p->nx, p->ny);
     return LBM_ERR_ARG;
   }
-  if (p->precision < LBM_PREC_F64 || p->precision > LBM_PREC_Q60) {
+  if (p->precision < LBM_PREC_F64 || p->precision > LBM_PREC_BF16SR) {
     set_error("%s: unknown precision %d", fn, p->precision);
     return LBM_ERR_ARG;
   }
@@ -376,8 +376,10 @@ extern "C" int lbm_pack_f64(int precision, const double* g, void* f, int nx, int
   switch (precision) {
     case LBM_PREC_F64: k_pack<StoreF64><<<nb, 256, 0, st>>>(g, (double*)f, nx, ny, sy, rho0); break;
     case LBM_PREC_F32: k_pack<StoreF32><<<nb, 256, 0, st>>>(g, (float*)f, nx, ny, sy, rho0); break;
-    case LBM_PREC_F16S: k_pack<StoreF16><<<nb, 256, 0, st>>>(g, (__half*)f, nx, ny, sy, rho0); break;
+    case LBM_PREC_F16S:
+    case LBM_PREC_F16SR: k_pack<StoreF16><<<nb, 256, 0, st>>>(g, (__half*)f, nx, ny, sy, rho0); break;
     case LBM_PREC_BF16S:
+    case LBM_PREC_BF16SR:
       k_pack<StoreBF16><<<nb, 256, 0, st>>>(g, (__nv_bfloat16*)f, nx, ny, sy, rho0);
       break;
     case LBM_PREC_Q60: k_pack<StoreQ60><<<nb, 256, 0, st>>>(g, (long long*)f, nx, ny, sy, rho0); break;
@@ -401,9 +403,11 @@ extern "C" int lbm_unpack_f64(int precision, const void* f, double* g, int nx, i
       k_unpack<StoreF32><<<nb, 256, 0, st>>>((const float*)f, g, nx, ny, sy, rho0);
       break;
     case LBM_PREC_F16S:
+    case LBM_PREC_F16SR:
       k_unpack<StoreF16><<<nb, 256, 0, st>>>((const __half*)f, g, nx, ny, sy, rho0);
       break;
     case LBM_PREC_BF16S:
+    case LBM_PREC_BF16SR:
       k_unpack<StoreBF16><<<nb, 256, 0, st>>>((const __nv_bfloat16*)f, g, nx, ny, sy, rho0);
       break;
     case LBM_PREC_Q60:

@@ -180,6 +180,8 @@ int batch_enqueue(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) 
     case LBM_PREC_F32: enqueue_store<StoreF32>(b, n_steps, parity, st); break;
     case LBM_PREC_F16S: enqueue_store<StoreF16>(b, n_steps, parity, st); break;
     case LBM_PREC_Q60: enqueue_store<StoreQ60>(b, n_steps, parity, st); break;
+    case LBM_PREC_F16SR: enqueue_store<StoreF16SR>(b, n_steps, parity, st); break;
+    case LBM_PREC_BF16SR: enqueue_store<StoreBF16SR>(b, n_steps, parity, st); break;
     default: enqueue_store<StoreBF16>(b, n_steps, parity, st); break;
   }
   cudaError_t e = cudaGetLastError();

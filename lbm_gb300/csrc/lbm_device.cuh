@@ -46,37 +46,137 @@ __device__ __forceinline__ float recip(float x) { return 1.0f / x; }
 // Storage forms.  Full-precision values are T (double for F64, float for the
 // reduced forms); shifted forms store d = f - w_q * rho0.
 // ---------------------------------------------------------------------------
+// store_r(p, v, r): the store of a kernel's update, given 32 random bits r;
+// only the stochastic-rounding forms use r.
 struct StoreF64 {
   using S = double;
   using T = double;
   static constexpr bool kShift = false;
   static constexpr bool kFixed = false;
+  static constexpr bool kStochastic = false;
   __device__ static T load(const S* p) { return *p; }
   __device__ static void store(S* p, T v) { *p = v; }
+  __device__ static void store_r(S* p, T v, unsigned) { *p = v; }
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned) { p[0] = v0; p[1] = v1; }
 };
 struct StoreF32 {
   using S = float;
   using T = float;
   static constexpr bool kShift = true;
   static constexpr bool kFixed = false;
+  static constexpr bool kStochastic = false;
   __device__ static T load(const S* p) { return *p; }
   __device__ static void store(S* p, T v) { *p = v; }
+  __device__ static void store_r(S* p, T v, unsigned) { *p = v; }
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned) { p[0] = v0; p[1] = v1; }
 };
 struct StoreF16 {
   using S = __half;
   using T = float;
   static constexpr bool kShift = true;
   static constexpr bool kFixed = false;
+  static constexpr bool kStochastic = false;
   __device__ static T load(const S* p) { return __half2float(*p); }
   __device__ static void store(S* p, T v) { *p = __float2half_rn(v); }
+  __device__ static void store_r(S* p, T v, unsigned) { *p = __float2half_rn(v); }
+  // p[0] = v0, p[1] = v1 (p 4-byte aligned), one packed conversion.
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned) {
+    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v0, v1);
+  }
 };
 struct StoreBF16 {
   using S = __nv_bfloat16;
   using T = float;
   static constexpr bool kShift = true;
   static constexpr bool kFixed = false;
+  static constexpr bool kStochastic = false;
   __device__ static T load(const S* p) { return __bfloat162float(*p); }
   __device__ static void store(S* p, T v) { *p = __float2bfloat16_rn(v); }
+  __device__ static void store_r(S* p, T v, unsigned) { *p = __float2bfloat16_rn(v); }
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v0, v1);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Stochastic rounding for the 16-bit forms.  Round-to-nearest storage loses
+// every per-iteration change of a population smaller than half an ulp of its
+// deviation, which damps slow dynamics (vortex shedding amplitude in a
+// cylinder wake); rounding up with probability equal to the discarded
+// fraction keeps those changes in expectation.  FP32 -> FP16: add 13 random
+// bits below the 10 kept mantissa bits and truncate; FP32 -> BF16: 16 bits
+// below 7.  Values below the FP16 normal range (|v| < 2^-14) or near its top
+// round to nearest.  The random bits come from a deterministic hash of
+// (cell, iteration) advanced by xorshift32 per store, so runs are repeatable.
+// ---------------------------------------------------------------------------
+// 32-bit integer hash "lowbias32" (C. Wellons, hash-prospector, public domain).
+__device__ __forceinline__ unsigned hash32(unsigned x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+// xorshift32 (G. Marsaglia, "Xorshift RNGs", J. Stat. Softw. 8(14), 2003).
+__device__ __forceinline__ unsigned xorshift32(unsigned x) {
+  x ^= x << 13;
+  x ^= x >> 17;
+  x ^= x << 5;
+  return x;
+}
+// Random state of one cell at one iteration (never zero).
+__device__ __forceinline__ unsigned sr_seed(long long cell, long long it) {
+  return hash32((unsigned)cell ^ hash32((unsigned)it * 0x9e3779b9u + 0x632be5abu)) | 1u;
+}
+__device__ __forceinline__ __half half_sr(float v, unsigned r) {
+  const unsigned b = __float_as_uint(v), mag = b & 0x7fffffffu;
+  if (mag < 0x38800000u || mag >= 0x477fe000u) return __float2half_rn(v);
+  return __float2half_rz(__uint_as_float(b + (r & 0x1fffu)));
+}
+__device__ __forceinline__ __nv_bfloat16 bf16_sr(float v, unsigned r) {
+  const unsigned b = __float_as_uint(v), mag = b & 0x7fffffffu;
+  if (mag < 0x00800000u || mag >= 0x7f7f0000u) return __float2bfloat16_rn(v);
+  return __float2bfloat16_rz(__uint_as_float(b + (r & 0xffffu)));
+}
+// Linear congruential step (constants of Numerical Recipes, 2nd ed., 7.1);
+// only its upper bits are used as dither.
+__device__ __forceinline__ unsigned lcg32(unsigned x) { return x * 1664525u + 1013904223u; }
+
+// Packed stochastic rounding of a pair (bulk kernel): dithers from one LCG
+// state, bits 19..31 and 6..18 for FP16; bits 16..31 and, after one more LCG
+// step, 16..31 for BF16.  No range check: the bulk values are deviations far
+// below the FP16 maximum, and below 2^-14 (FP16 subnormals) the dither is
+// smaller than the FP16 step, a bias below 6e-8.
+__device__ __forceinline__ unsigned f16x2_rz(float lo, float hi) {
+  unsigned d;
+  asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+__device__ __forceinline__ unsigned bf16x2_rz(float lo, float hi) {
+  unsigned d;
+  asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
+struct StoreF16SR : StoreF16 {
+  static constexpr bool kStochastic = true;
+  __device__ static void store_r(S* p, T v, unsigned r) { *p = half_sr(v, r); }
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned r) {
+    const float a = __uint_as_float(__float_as_uint(v0) + (r >> 19));
+    const float b = __uint_as_float(__float_as_uint(v1) + ((r >> 6) & 0x1fffu));
+    *reinterpret_cast<unsigned*>(p) = f16x2_rz(a, b);
+  }
+};
+struct StoreBF16SR : StoreBF16 {
+  static constexpr bool kStochastic = true;
+  __device__ static void store_r(S* p, T v, unsigned r) { *p = bf16_sr(v, r); }
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned r) {
+    const unsigned r2 = lcg32(r);
+    const float a = __uint_as_float(__float_as_uint(v0) + (r >> 16));
+    const float b = __uint_as_float(__float_as_uint(v1) + (r2 >> 16));
+    *reinterpret_cast<unsigned*>(p) = bf16x2_rz(a, b);
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -133,8 +233,14 @@ struct StoreQ60 {
   using T = double;
   static constexpr bool kShift = false;
   static constexpr bool kFixed = true;
+  static constexpr bool kStochastic = false;
   __device__ static T load(const S* p) { return q60_to_double(*p); }
   __device__ static void store(S* p, T v) { *p = q60_from_double(v); }
+  __device__ static void store_r(S* p, T v, unsigned) { *p = q60_from_double(v); }
+  __device__ static void store_pair(S* p, T v0, T v1, unsigned) {
+    p[0] = q60_from_double(v0);
+    p[1] = q60_from_double(v1);
+  }
 };
 
 // Signed 64 x 64 -> high 64 multiply from three 32 x 32 -> 64 products.

@@ -221,6 +221,8 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
       case LBM_PREC_F32: launch_store<StoreF32>(a, mode, st, e); break;
       case LBM_PREC_F16S: launch_store<StoreF16>(a, mode, st, e); break;
       case LBM_PREC_Q60: launch_store<StoreQ60>(a, mode, st, e); break;
+      case LBM_PREC_F16SR: launch_store<StoreF16SR>(a, mode, st, e); break;
+      case LBM_PREC_BF16SR: launch_store<StoreBF16SR>(a, mode, st, e); break;
       default: launch_store<StoreBF16>(a, mode, st, e); break;
     }
   }

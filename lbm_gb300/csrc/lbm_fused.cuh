@@ -205,8 +205,12 @@ __device__ __forceinline__ void bulk_cell(const FusedArgs& a, long long cell) {
   if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
   collide<T, St::kShift>(d, m, k);
   S* fout = (S*)a.fout;
+  unsigned r = St::kStochastic ? sr_seed(cell, *a.it_dev) : 0u;
 #pragma unroll
-  for (int q = 0; q < 9; ++q) St::store(fout + q * Ns + cell, d[q]);
+  for (int q = 0; q < 9; ++q) {
+    if (St::kStochastic) r = xorshift32(r);
+    St::store_r(fout + q * Ns + cell, d[q], r);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -271,38 +275,49 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
   if (!active) return;
 
   P out[9];
+  // Cells are updated two at a time so that each plane's pair of results is
+  // converted and rounded by one packed instruction (St::store_pair).
+  unsigned r = St::kStochastic ? sr_seed(gi, *a.it_dev) : 0u;
 #pragma unroll
-  for (int e = 0; e < V; ++e) {
-    T d[9];
+  for (int e = 0; e < V; e += 2) {
+    T dd[2][9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      if (cy(q) == 1) {
-        d[q] = e == 0 ? halo[q] : St::load(&in[q].v[e - 1]);
-      } else if (cy(q) == -1) {
-        d[q] = e == V - 1 ? halo[q] : St::load(&in[q].v[e + 1]);
-      } else {
-        d[q] = St::load(&in[q].v[e]);
+    for (int h = 0; h < 2; ++h) {
+      const int c = e + h;
+      T* d = dd[h];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        if (cy(q) == 1) {
+          d[q] = c == 0 ? halo[q] : St::load(&in[q].v[c - 1]);
+        } else if (cy(q) == -1) {
+          d[q] = c == V - 1 ? halo[q] : St::load(&in[q].v[c + 1]);
+        } else {
+          d[q] = St::load(&in[q].v[c]);
+        }
+      }
+      Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+      const int j = j0 + c;
+      if (j < ny && a.write_macro) {
+        const long long rc = (long long)i * ny + j;
+        a.rho_out[rc] = (double)m.rho;
+        a.u_out[rc] = (double)m.ux;
+        a.u_out[N + rc] = (double)m.uy;
+      }
+      // Wall cells are checked by k_special, which recomputes them.
+      if (a.check_finite && j > 0 && j < ny - 1 && !isfinite(m.rho + m.ux + m.uy))
+        atomicOr(a.status, 1u);
+      collide<T, St::kShift>(d, m, k);
+      if (j >= ny) {
+        // padding: keep the stored deviations at zero (never read by a cell)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) d[q] = T(0);
       }
     }
-    Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
-    const int j = j0 + e;
-    if (j < ny && a.write_macro) {
-      const long long rc = (long long)i * ny + j;
-      a.rho_out[rc] = (double)m.rho;
-      a.u_out[rc] = (double)m.ux;
-      a.u_out[N + rc] = (double)m.uy;
-    }
-    // Wall cells are checked by k_special, which recomputes them.
-    if (a.check_finite && j > 0 && j < ny - 1 && !isfinite(m.rho + m.ux + m.uy))
-      atomicOr(a.status, 1u);
-    collide<T, St::kShift>(d, m, k);
-    if (j >= ny) {
-      // padding: keep the stored deviations at zero (never read by a cell)
 #pragma unroll
-      for (int q = 0; q < 9; ++q) d[q] = T(0);
+    for (int q = 0; q < 9; ++q) {
+      if (St::kStochastic) r = lcg32(r);
+      St::store_pair(&out[q].v[e], dd[0][q], dd[1][q], r);
     }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) St::store(&out[q].v[e], d[q]);
   }
   S* fout = (S*)a.fout;
 #pragma unroll
@@ -569,8 +584,12 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
   if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
   collide<T, St::kShift>(d, m, k);
   S* fout = (S*)a.fout;
+  unsigned r = St::kStochastic ? sr_seed(scell, *a.it_dev) : 0u;
 #pragma unroll
-  for (int q = 0; q < 9; ++q) St::store(fout + q * a.Ns + scell, d[q]);
+  for (int q = 0; q < 9; ++q) {
+    if (St::kStochastic) r = xorshift32(r);
+    St::store_r(fout + q * a.Ns + scell, d[q], r);
+  }
 }
 
 // Per-obstacle drag/lift: one block (256 threads) per obstacle, fixed-order

@@ -2,7 +2,7 @@
 
 ``FusedEngine`` owns the device state of one lattice run: two ping-pong
 buffers of post-collision populations in the storage form (``f64``, ``q60``,
-``f32``, ``f16s``, ``bf16s``), the special-cell and link tables, the scratch that the
+``f32``, ``f16s``, ``bf16s``, ``f16sr``, ``bf16sr``), the special-cell and link tables, the scratch that the
 kernels carry from one iteration to the next, the per-iteration drag/lift
 history and the BC schedule.  It drives ``lbm_advance`` /
 ``lbm_advance_graph`` of liblbm_gb300 (include/lbm_gb300.h).
@@ -29,6 +29,8 @@ _STORE_DTYPE = {
     "f16s": torch.float16,
     "bf16s": torch.bfloat16,
     "q60": torch.int64,
+    "f16sr": torch.float16,
+    "bf16sr": torch.bfloat16,
 }
 
 WALL_OPS = {
