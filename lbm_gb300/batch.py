@@ -120,7 +120,7 @@ def re_max_stable(ny, u_lbm, tau_min=0.53):
 class Batch:
     """One fused engine per app, advanced together through lbm_batch."""
 
-    def __init__(self, apps, precision="f16s", config=None, max_steps=20000, verbose=False):
+    def __init__(self, apps, precision="f16sr", config=None, max_steps=20000, verbose=False):
         self.apps = list(apps)
         self.precision = precision
         self.lattices, self.engines = [], []

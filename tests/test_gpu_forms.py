@@ -1,11 +1,17 @@
 """Reduced-precision storage forms against the plain FP64 path.
 
-FP32, FP16-shifted and BF16-shifted storage (FP32 arithmetic) run the same
-fused kernels; their error is stated against the FP64 run of the same case.
+FP32, FP16-shifted and BF16-shifted storage (FP32 arithmetic), with
+round-to-nearest or stochastic rounding (f16sr, bf16sr), run the same fused
+kernels; their error is stated against the FP64 run of the same case.
 Bounds are about three times the errors measured on a GB300 (FP32 u L2
-3.4e-5 / 5.5e-5; FP16 2.5e-3 / 4.8e-3 with mean Cd 1.5e-4; BF16 0.099 /
-0.099 with mean Cd 1.3e-2).  The lattices have ny % 8 == 0, so the
-vectorised bulk kernel (16-byte loads, warp-shuffle halos) is the one tested.
+3.4e-5 / 5.5e-5; FP16 2.5e-3 / 2.0e-3 with mean Cd 5e-5; FP16 with
+stochastic rounding 2.8e-4 / 2.9e-3 with mean Cd 1.1e-4 and rms Cl 1.6e-4;
+BF16 0.099 / 0.15 with mean Cd 1.8e-2).  BF16 with stochastic rounding is
+left out of the Turek case: at tau = 0.515 its rounding noise (8-bit
+significand) drives the weakly damped non-hydrodynamic modes unstable; at
+tau = 0.548 (the 1100x200 channel of the benchmark) it runs and halves the
+BF16 mean-Cd error.  The lattices have ny % 8 == 0, so the vectorised bulk
+kernel (16-byte loads, warp-shuffle halos) is the one tested.
 """
 import numpy as np
 import pytest
@@ -19,7 +25,11 @@ BOUNDS = {
     "f32": (2e-4, 3e-4, 1e-4, 3e-4),
     "f16s": (1e-2, 2e-2, 1e-3, 1e-2),
     "bf16s": (0.3, 0.3, 5e-2, 0.25),
+    "f16sr": (1e-3, 1e-2, 5e-4, 1e-3),
+    "bf16sr": (0.3, None, None, None),
 }
+FORMS = ["f32", "f16s", "bf16s", "f16sr", "bf16sr"]
+TUREK_FORMS = ["f32", "f16s", "bf16s", "f16sr"]
 
 
 def _cavity():
@@ -52,7 +62,7 @@ def _u_err(out, ref):
     return float(np.linalg.norm(out["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
 
 
-@pytest.mark.parametrize("form", ["f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("form", FORMS)
 def test_cavity_form_error(fp64_runs, form):
     ref = fp64_runs["cavity"][0]
     out, _, _ = run_gpu(_cavity(), fused=True, precision=form)
@@ -60,7 +70,7 @@ def test_cavity_form_error(fp64_runs, form):
     assert _u_err(out, ref) <= BOUNDS[form][0]
 
 
-@pytest.mark.parametrize("form", ["f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("form", TUREK_FORMS)
 def test_turek_form_error(fp64_runs, form):
     ref, href, _ = fp64_runs["turek"]
     out, h, _ = run_gpu(_turek(), fused=True, precision=form)
@@ -73,7 +83,7 @@ def test_turek_form_error(fp64_runs, form):
     assert abs(cl_rms - cl_rms_ref) / cl_rms_ref <= BOUNDS[form][3]
 
 
-@pytest.mark.parametrize("form", ["f32", "f16s"])
+@pytest.mark.parametrize("form", ["f32", "f16s", "f16sr"])
 def test_padded_rows(cuda, form):
     """ny = 70 is not a multiple of the vector width: rows are padded to 72."""
     def mk():
@@ -88,9 +98,11 @@ def test_padded_rows(cuda, form):
     assert _u_err(out, ref) <= BOUNDS[form][0]
 
 
-def test_reduced_forms_are_deterministic(cuda):
-    """Two FP16 runs of the same case are bit-identical (fixed-order reductions)."""
-    a, ha, _ = run_gpu(_turek(), fused=True, precision="f16s")
-    b, hb, _ = run_gpu(_turek(), fused=True, precision="f16s")
+@pytest.mark.parametrize("form", ["f16s", "f16sr"])
+def test_reduced_forms_are_deterministic(cuda, form):
+    """Two FP16 runs of the same case are bit-identical (fixed-order reductions;
+    the stochastic rounding draws its bits from a hash of cell and iteration)."""
+    a, ha, _ = run_gpu(_turek(), fused=True, precision=form)
+    b, hb, _ = run_gpu(_turek(), fused=True, precision=form)
     assert np.array_equal(a["g"], b["g"])
     assert np.array_equal(ha, hb)
