@@ -25,7 +25,9 @@ BOUNDS = {
     "f32": (2e-4, 3e-4, 1e-4, 3e-4),
     "f16s": (1e-2, 2e-2, 1e-3, 1e-2),
     "bf16s": (0.3, 0.3, 5e-2, 0.25),
-    "f16sr": (1e-3, 1e-2, 5e-4, 1e-3),
+    # stochastic rounding: trajectories depend on the dither sequence, so the
+    # bounds leave room for it; the mean-Cd bound is the 1e-3 target itself
+    "f16sr": (2e-3, 2e-2, 1e-3, 5e-3),
     "bf16sr": (0.3, None, None, None),
 }
 FORMS = ["f32", "f16s", "bf16s", "f16sr", "bf16sr"]
