@@ -130,8 +130,10 @@ int lbm_zou_he_corner_f64(int corner, double* u, double* rho, double* g, int nx,
  * Special cells = every wall cell plus every fluid cell that owns an obstacle
  * link; they are re-done by a second kernel that applies, in reference order,
  * the links (IBB/BB), the wall operations and the corners.  The host supplies
- * the special-cell table (sorted linear cell indices i*ny + j, CSR offsets
- * into the link arrays, the special index of each corner's x-neighbour).
+ * the special-cell table (linear cell indices i*ny + j, each once; the
+ * Python host sorts them, which keeps a warp's cells close together), CSR
+ * offsets into the link arrays and the special index of each corner's
+ * x-neighbour.
  */
 typedef struct lbm_problem {
   int32_t nx, ny;
@@ -259,6 +261,8 @@ typedef struct lbm_batch_config {
                                     queue; 0: one block per tile                  */
   int32_t vec_bytes;             /* 8 or 16: bytes per vector access of the bulk
                                     kernel (cells per thread = this / element)    */
+  int32_t tile_rounds;           /* 1..64: a vector bulk tile is this many block-
+                                    widths of groups (a thread loops over them)   */
 } lbm_batch_config;
 int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32_t n_cases,
                      const lbm_batch_config* cfg);

@@ -11,6 +11,7 @@
   persistent special-cell kernel and one drag kernel.
 * ``autotune(batch)``  picks the scheduling (persistent work queue or one
   block per tile), the vector width of the bulk kernel (cells per thread),
+  block-widths per bulk tile,
   threads per block, persistent grid size and the number of iterations per
   CUDA graph by timing candidates on the batch.
 """
@@ -154,7 +155,8 @@ class Batch:
         arr = (_lib.Problem * len(self.engines))(*[e.P for e in self.engines])
         c = _lib.BatchConfig(cfg["bulk_threads"], cfg["bulk_blocks_per_sm"],
                              cfg["special_blocks_per_sm"], cfg["scalar_tile_cells"],
-                             int(cfg.get("persistent", 1)), int(cfg.get("vec_bytes", 16)))
+                             int(cfg.get("persistent", 1)), int(cfg.get("vec_bytes", 16)),
+                             int(cfg.get("tile_rounds", 1)))
         h = ctypes.c_void_p()
         _lib.call("lbm_batch_create", ctypes.byref(h), arr, len(self.engines), ctypes.byref(c))
         self.handle = h
@@ -194,7 +196,8 @@ class Batch:
 
 def default_config():
     return {"bulk_threads": 128, "bulk_blocks_per_sm": 8, "special_blocks_per_sm": 8,
-            "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 1, "vec_bytes": 16}
+            "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 0, "vec_bytes": 8,
+            "tile_rounds": 4}
 
 
 def time_batch(batch, n_steps, k=None):
@@ -216,20 +219,25 @@ def autotune(batch, steps=60, space=None, verbose=False):
     also captures its graph); the lattices keep advancing, which does not
     change the cost per iteration.  Returns (best config, table of trials).
     """
-    space = space or {
-        "persistent": [1, 0],
-        "vec_bytes": [16, 8],
-        "bulk_threads": [64, 128, 256],
-        "bulk_blocks_per_sm": [4, 8],
-        "special_blocks_per_sm": [8],
-        "k_steps": [50],
-    }
-    keys = list(space)
+    # one block per tile (the persistent grid size does not apply), then
+    # persistent blocks; a dict of value lists or a list of such dicts
+    space = space or [
+        {"persistent": [0], "tile_rounds": [2, 4, 8], "vec_bytes": [16, 8],
+         "bulk_threads": [64, 128], "k_steps": [50]},
+        {"persistent": [1], "tile_rounds": [4, 8], "vec_bytes": [16, 8],
+         "bulk_threads": [128], "bulk_blocks_per_sm": [8, 12], "k_steps": [50]},
+    ]
+    spaces = [space] if isinstance(space, dict) else list(space)
+    candidates = []
+    for sp in spaces:
+        keys = list(sp)
+        for values in itertools.product(*(sp[k] for k in keys)):
+            candidates.append(dict(zip(keys, values)))
     trials = []
     best = None
-    for values in itertools.product(*(space[k] for k in keys)):
+    for values in candidates:
         cfg = default_config()
-        cfg.update(dict(zip(keys, values)))
+        cfg.update(values)
         batch.set_config(cfg)
         k = cfg["k_steps"]
         batch.advance(k, k=k)  # warm-up + graph capture

@@ -32,7 +32,7 @@ struct lbm_batch {
   int n_special_tiles;
   int2* d_drag_items;       // (case, obstacle)
   int n_drag_items;
-  unsigned* d_queue;        // [0] bulk queue, [1] special queue
+  unsigned* d_queue;        // [0] bulk queue, [1] special queue, [2] step-done count
   long long* d_it;          // shared iteration counter
   int any_scalar;
   // graph cache (one per (n_steps, parity))
@@ -44,6 +44,14 @@ namespace lbm {
 namespace {
 
 
+// One vector group per thread per round; a tile is tile_rounds block-widths
+// of groups (whole warps in every round: only a lattice's last tile is
+// shorter, and the groups past the lattice's end are inactive).
+template <class St, int V>
+__device__ __forceinline__ void bulk_tile_vec(const FusedArgs& a, const int4& tl) {
+  for (int g = 0; g < tl.z; g += blockDim.x) bulk_group_vec<St, V>(a, (long long)tl.y + g + threadIdx.x);
+}
+
 // VB: bytes per vector access (a group of VB / sizeof(element) cells per
 // thread; lbm_batch_config.vec_bytes).  kVecOnly: every tile is a vector
 // tile (no scalar path compiled in).
@@ -54,22 +62,25 @@ __global__ void __launch_bounds__(256) k_batch_bulk(const FusedArgs* __restrict_
   constexpr int V = VB / (int)sizeof(typename St::S);
   if (blockIdx.x == 0 && threadIdx.x == 0)
     queue[1] = 0;  // the special phase of this iteration starts from tile 0
+  // the next tile is taken while this one is processed
   __shared__ int t_sh;
-  for (;;) {
-    if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[0], 1u);
-    __syncthreads();
-    const int t = t_sh;
-    __syncthreads();
-    if (t >= n_tiles) break;
+  if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[0], 1u);
+  __syncthreads();
+  for (int t = t_sh; t < n_tiles;) {
+    int next = 0;
+    if (threadIdx.x == 0) next = (int)atomicAdd(&queue[0], 1u);
     const int4 tl = tiles[t];
     const FusedArgs& a = args[tl.x];
     if (tl.w) {
-      // one vector group per thread; tiles are blockDim groups long
-      bulk_group_vec<St, V>(a, (long long)tl.y + threadIdx.x);
+      bulk_tile_vec<St, V>(a, tl);
     } else if (!kVecOnly) {
       for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
         bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
     }
+    __syncthreads();
+    if (threadIdx.x == 0) t_sh = next;
+    __syncthreads();
+    t = t_sh;
   }
   if (last) advance_counter(it_dev, queue + 2);
 }
@@ -86,7 +97,7 @@ __global__ void __launch_bounds__(256) k_batch_bulk_grid(const FusedArgs* __rest
   const int4 tl = tiles[blockIdx.x];
   const FusedArgs& a = args[tl.x];
   if (tl.w) {
-    bulk_group_vec<St, V>(a, (long long)tl.y + threadIdx.x);
+    bulk_tile_vec<St, V>(a, tl);
   } else if (!kVecOnly) {
     for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
       bulk_cell<St, LBM_MODE_STEP>(a, (long long)tl.y + k);
@@ -95,7 +106,7 @@ __global__ void __launch_bounds__(256) k_batch_bulk_grid(const FusedArgs* __rest
 }
 
 template <class St>
-__global__ void __launch_bounds__(128) k_batch_special_grid(const FusedArgs* __restrict__ args,
+__global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_batch_special_grid(const FusedArgs* __restrict__ args,
                                                             const int4* __restrict__ tiles,
                                                             unsigned* queue, long long* it_dev,
                                                             int last) {
@@ -106,21 +117,24 @@ __global__ void __launch_bounds__(128) k_batch_special_grid(const FusedArgs* __r
 }
 
 template <class St>
-__global__ void __launch_bounds__(128) k_batch_special(const FusedArgs* __restrict__ args,
+__global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_batch_special(const FusedArgs* __restrict__ args,
                                                        const int4* __restrict__ tiles, int n_tiles,
                                                        unsigned* queue, long long* it_dev,
                                                        int last) {
   if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;  // next iteration's bulk queue
   __shared__ int t_sh;
-  for (;;) {
-    if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[1], 1u);
-    __syncthreads();
-    const int t = t_sh;
-    __syncthreads();
-    if (t >= n_tiles) break;
+  if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[1], 1u);
+  __syncthreads();
+  for (int t = t_sh; t < n_tiles;) {
+    int next = 0;
+    if (threadIdx.x == 0) next = (int)atomicAdd(&queue[1], 1u);
     const int4 tl = tiles[t];
     for (int k = threadIdx.x; k < tl.z; k += blockDim.x)
       special_cell<St, LBM_MODE_STEP>(args[tl.x], tl.y + k);
+    __syncthreads();
+    if (threadIdx.x == 0) t_sh = next;
+    __syncthreads();
+    t = t_sh;
   }
   if (last) advance_counter(it_dev, queue + 2);
 }
@@ -229,7 +243,8 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       cfg->special_blocks_per_sm < 1 || cfg->special_blocks_per_sm > 32 ||
       cfg->scalar_tile_cells < 32 || cfg->scalar_tile_cells > (1 << 20) ||
       (cfg->persistent != 0 && cfg->persistent != 1) ||
-      (cfg->vec_bytes != 8 && cfg->vec_bytes != 16)) {
+      (cfg->vec_bytes != 8 && cfg->vec_bytes != 16) || cfg->tile_rounds < 1 ||
+      cfg->tile_rounds > 64) {
     set_error("lbm_batch_create: bad config (threads %d, blocks/SM %d/%d, tile %d)",
               cfg->bulk_threads, cfg->bulk_blocks_per_sm, cfg->special_blocks_per_sm,
               cfg->scalar_tile_cells);
@@ -270,8 +285,10 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
     const long long N = (long long)p.nx * sy;  // storage cells, padding included
     if (V > 1 && sy % V == 0) {
       const long long groups = (long long)p.nx * (sy / V);
-      for (long long g = 0; g < groups; g += cfg->bulk_threads)
-        bulk.push_back(make_int4(c, (int)g, (int)std::min<long long>(cfg->bulk_threads, groups - g), 1));
+      // tile_rounds block-widths of groups per tile
+      const int tg = cfg->bulk_threads * cfg->tile_rounds;
+      for (long long g = 0; g < groups; g += tg)
+        bulk.push_back(make_int4(c, (int)g, (int)std::min<long long>(tg, groups - g), 1));
     } else {
       for (long long x = 0; x < N; x += cfg->scalar_tile_cells)
         bulk.push_back(make_int4(c, (int)x, (int)std::min<long long>(cfg->scalar_tile_cells, N - x), 0));

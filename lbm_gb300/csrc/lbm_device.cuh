@@ -125,9 +125,16 @@ __device__ __forceinline__ unsigned xorshift32(unsigned x) {
   x ^= x << 5;
   return x;
 }
-// Random state of one cell at one iteration (never zero).
+// Random state of one cell at one iteration (never zero): sr_cell of the
+// cell's storage index and sr_iter of the iteration.
+__device__ __forceinline__ unsigned sr_iter(long long it) {
+  return hash32((unsigned)it * 0x9e3779b9u + 0x632be5abu);
+}
+__device__ __forceinline__ unsigned sr_cell(long long cell, unsigned it_hash) {
+  return hash32((unsigned)cell ^ it_hash) | 1u;
+}
 __device__ __forceinline__ unsigned sr_seed(long long cell, long long it) {
-  return hash32((unsigned)cell ^ hash32((unsigned)it * 0x9e3779b9u + 0x632be5abu)) | 1u;
+  return sr_cell(cell, sr_iter(it));
 }
 __device__ __forceinline__ __half half_sr(float v, unsigned r) {
   const unsigned b = __float_as_uint(v), mag = b & 0x7fffffffu;

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256, LBM_Q60_MIN_BLOCKS) k_bulk_q60(FusedArgs 
 }
 
 template <class St, int MODE>
-__global__ void __launch_bounds__(128) k_special(FusedArgs a) {
+__global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_special(FusedArgs a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < a.n_special) special_cell<St, MODE>(a, s);
   if (a.advance_at == 1) advance_counter(a.it_dev, a.step_done);

@@ -276,10 +276,13 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
 
   P out[9];
   // Cells are updated two at a time so that each plane's pair of results is
-  // converted and rounded by one packed instruction (St::store_pair).
-  unsigned r = St::kStochastic ? sr_seed(gi, *a.it_dev) : 0u;
+  // converted and rounded by one packed instruction (St::store_pair).  The
+  // random stream of a pair starts from its first cell's storage index, so
+  // the bits do not depend on V.
+  const unsigned it_hash = St::kStochastic ? sr_iter(*a.it_dev) : 0u;
 #pragma unroll
   for (int e = 0; e < V; e += 2) {
+    unsigned r = St::kStochastic ? sr_cell((long long)i * sy + j0 + e, it_hash) : 0u;
     T dd[2][9];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -337,6 +340,12 @@ __device__ __forceinline__ typename St::T full_value(const typename St::S* p, in
   const T v = St::load(p);
   return St::kShift ? v + T(wgt(q)) * rho0 : v;
 }
+
+// Resident 128-thread blocks per SM that the special-cell kernels are
+// compiled for (register cap 65536 / (128 x this)).
+#ifndef LBM_SPECIAL_MIN_BLOCKS
+#define LBM_SPECIAL_MIN_BLOCKS 5
+#endif
 
 __device__ __forceinline__ bool is_corner_neighbour(const FusedArgs& a, int s) {
   bool r = false;
@@ -398,16 +407,15 @@ __device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<typenam
       } else {
         ibb_coefs<T>(p, c1, c2, c3);
       }
-      if (p < T(0.5)) {
-        const long long x2 = a.link_nb2[k];
-        const T up_q_1 = full_value<St>(fin + q * Ns + x1, q, rho0);
-        const T up_q_2 = full_value<St>(fin + q * Ns + x2, q, rho0);
-        v = c1 * up_q_x + c2 * up_q_1 - c3 * up_q_2;
-      } else {
-        const T up_qb_x = full_value<St>(fin + qb * Ns + x, qb, rho0);
-        const T up_qb_1 = full_value<St>(fin + qb * Ns + x1, qb, rho0);
-        v = c1 * up_q_x + c2 * up_qb_x + c3 * up_qb_1;
-      }
+      // p < 1/2: c1 f_q(x) + c2 f_q(x1) - c3 f_q(x2);
+      // else:    c1 f_q(x) + c2 f_qb(x) + c3 f_qb(x1).  One load pattern.
+      const bool near = p < T(0.5);
+      const int qy = near ? q : qb;
+      const long long y1 = qy * Ns + (near ? x1 : x);
+      const long long y2 = qy * Ns + (near ? a.link_nb2[k] : x1);
+      const T u1 = full_value<St>(fin + y1, qy, rho0);
+      const T u2 = full_value<St>(fin + y2, qy, rho0);
+      v = c1 * up_q_x + c2 * u1 + (near ? -c3 : c3) * u2;
     }
     set_pop<T>(c.g, qb, v);
   }

@@ -396,6 +396,9 @@ class FusedEngine:
             raise FloatingPointError("non-finite density or velocity in the lattice")
         if s & 2:
             raise RuntimeError("BC schedule table does not cover the iterations run")
+        if s & 4:
+            raise RuntimeError("batched step: special-cell tiles stopped waiting for "
+                               "their lattice's bulk tiles")
 
     # --------------------------------------------------------- snapshot/restore
     def snapshot(self):

@@ -1,12 +1,13 @@
 """Batched lattices: a lattice advanced inside a batch gives the same bits as
 the same lattice advanced alone (same per-cell code, its own tables and
 scratch), for vectorised (ny % 8 == 0) and scalar tiles, cavities and IBB
-channels, FP16-shifted and FP64 storage."""
+channels, FP16-shifted, fixed-point and FP64 storage, and each scheduling
+of the batch kernels."""
 import numpy as np
 import pytest
 
 from lbm_gb300.apps import cavity
-from lbm_gb300.batch import Batch, channel_squares, sweep_apps
+from lbm_gb300.batch import Batch, channel_squares, default_config, sweep_apps
 from lbm_gb300.run import _finalize_state
 
 pytestmark = pytest.mark.gpu
@@ -36,10 +37,16 @@ def _finish(batch, steps):
     return res
 
 
-@pytest.mark.parametrize("precision", ["f16s", "f64"])
-def test_batch_equals_single_lattices(cuda, precision):
+# persistent: 1 work-queue kernels, 0 one block per tile; rounds: block-widths
+# of vector groups per bulk tile.
+@pytest.mark.parametrize("precision,persistent,vec_bytes,rounds", [
+    ("f16s", 1, 16, 1), ("f64", 1, 16, 1), ("f16sr", 0, 8, 1), ("f16sr", 1, 8, 4),
+    ("f16sr", 0, 16, 3), ("q60", 0, 16, 1)])
+def test_batch_equals_single_lattices(cuda, precision, persistent, vec_bytes, rounds):
     steps = 120
-    b = Batch(_apps(), precision=precision)
+    cfg = default_config()
+    cfg.update(persistent=persistent, vec_bytes=vec_bytes, bulk_threads=64, tile_rounds=rounds)
+    b = Batch(_apps(), precision=precision, config=cfg)
     b.advance(steps, k=40)
     b.check()
     got = _finish(b, steps)
