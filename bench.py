@@ -517,6 +517,18 @@ def cpu_reference(ny, seconds, min_iters=2):
 
 
 # ---------------------------------------------------------------------------
+def replica_totals(ms, e2e_value, world, dist=None, device="cuda"):
+    """Whole-job figures of `world` independent replicas (one lattice per
+    GPU, no data exchange): the slowest rank's time per iteration, and
+    `world` x the slowest rank's end-to-end rate."""
+    if dist is None or world == 1:
+        return ms, e2e_value * world
+    import torch
+    t = torch.tensor([ms, -e2e_value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0]), -float(t[1]) * world
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -568,14 +580,7 @@ def main():
     del app, lat, eng, state
     torch.cuda.empty_cache()
 
-    ms = res["ms_per_step"]
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        e = torch.tensor([e2e["value"]], device="cuda")
-        dist.all_reduce(e, op=dist.ReduceOp.MIN)
-        e2e["value"] = float(e.item()) * world
+    ms, e2e["value"] = replica_totals(res["ms_per_step"], e2e["value"], world, dist)
     N = 4 * args.ny * args.ny
     value = N * world / (ms * 1e-3) / 1e6
 
