@@ -84,6 +84,9 @@ def parse():
     ap.add_argument("--sweep-steps", type=int, default=10000,
                     help="iterations of the 256-case batched sweep (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--array-errors", type=int, default=0,
+                    help="iterations of the obstacle-array workload in every form, errors "
+                         "against FP64 (0: skipped; 100000 takes ~7 minutes)")
     return ap.parse_args()
 
 
@@ -334,10 +337,20 @@ def channel_app(ny, steps):
 def run_channel(precision, ny, steps, tmp, chunk=2000):
     """Iterations 0 .. steps-1 of the channel in one form: drag/lift series
     (Cd, Cl of iterations 0 .. steps-2), final velocity field, MLUPS."""
+    app = channel_app(ny, steps)
+    r = run_case(app, precision, steps, tmp, chunk)
+    norm = -2.0 / (app.rho_lbm * app.D_lbm * app.u_avg ** 2)
+    r["cd"], r["cl"] = r.pop("fx") * norm, r.pop("fy") * norm
+    return r
+
+
+def run_case(app, precision, steps, tmp, chunk=2000):
+    """Iterations 0 .. steps-1 of an app in one form from its initial state:
+    drag/lift sums over every obstacle (iterations 0 .. steps-2), final
+    velocity field on the host, MLUPS."""
     import torch
     import lbm_gb300
     from lbm_gb300.engine import FusedEngine, trace_bc_program
-    app = channel_app(ny, steps)
     with contextlib.redirect_stdout(io.StringIO()):
         lat = lbm_gb300.lattice(app, precision=precision, output_dir=tmp, verbose=False)
         lat.generate_image = lambda obstacles: None
@@ -357,12 +370,50 @@ def run_channel(precision, ny, steps, tmp, chunk=2000):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     eng.check_status()
-    rows = eng.drag_rows(0, steps - 2)[:, 0, :]
-    norm = -2.0 / (app.rho_lbm * app.D_lbm * app.u_avg ** 2)
+    idx = torch.arange(0, steps - 1, device=eng.drag_hist.device) % eng.drag_cap
+    rows = eng.drag_hist[idx, :len(obstacles)].sum(dim=1).cpu().numpy()
     u = lat.device_field("u").cpu().numpy().copy()
     del eng
-    return {"cd": rows[:, 0] * norm, "cl": rows[:, 1] * norm, "u": u,
+    return {"fx": rows[:, 0], "fy": rows[:, 1], "u": u,
             "mlups": lat.nx * lat.ny * steps / dt / 1e6, "nx": lat.nx, "ny": lat.ny}
+
+
+def measure_array_errors(steps, forms, tmp, ny):
+    """Every form on the obstacle-array workload from the same initial state,
+    errors against the FP64 run: total drag (sum of fx over the obstacles)
+    mean / max and total lift rms over the second half, the total-drag series,
+    and the velocity field at the last iteration (L2)."""
+    import torch
+    ref = run_case(make_app(ny), "f64", steps, tmp)
+    half = slice(len(ref["fx"]) // 2, None)
+
+    def stats(r):
+        fx, fy = r["fx"][half], r["fy"][half]
+        return {"fx_mean": float(fx.mean()), "fx_max": float(np.abs(fx).max()),
+                "fy_rms": float(np.sqrt((fy ** 2).mean()))}
+
+    sref = stats(ref)
+    out = {"case": "obstacle_array %dx%d, 400 squares, Re 2000 on the side, %d iterations "
+                   "(all forms from the same initial state)" % (ref["nx"], ref["ny"], steps),
+           "f64": dict(sref, mlups=ref["mlups"])}
+    for form in forms:
+        if form == "f64":
+            continue
+        try:
+            r = run_case(make_app(ny), form, steps, tmp)
+        except FloatingPointError as e:  # the form's range or precision gave out
+            out[form] = {"diverged": str(e)}
+            torch.cuda.empty_cache()
+            continue
+        st = stats(r)
+        err = {k + "_rel": abs(st[k] - sref[k]) / abs(sref[k]) for k in sref}
+        err["u_l2_rel"] = float(np.linalg.norm(r["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
+        err["fx_series_max_rel"] = float(np.max(np.abs(r["fx"] - ref["fx"])) /
+                                         np.max(np.abs(ref["fx"])))
+        out[form] = dict(st, mlups=r["mlups"], error_vs_f64=err)
+        del r
+        torch.cuda.empty_cache()
+    return out
 
 
 def measure_form_errors(steps, forms, tmp, ny=200):
@@ -606,6 +657,11 @@ def main():
         form_errors = measure_form_errors(args.error_steps, FORMS, tmp)
         torch.cuda.empty_cache()
 
+    array_errors = None
+    if rank == 0 and args.array_errors > 0:
+        array_errors = measure_array_errors(args.array_errors, FORMS, tmp, args.ny)
+        torch.cuda.empty_cache()
+
     sweep = None
     if rank == 0 and args.sweep_steps > 0:
         sweep = measure_sweep(args.sweep_steps)
@@ -642,6 +698,7 @@ def main():
         "kernel_ms": res["kernel_ms"], "e2e": e2e,
         "gpu_launches": args.steps * res["kernels_per_step"],
         "clocks": clocks, "forms": forms, "form_errors": form_errors,
+        "array_form_errors": array_errors,
         "batched_sweep": sweep, "adjoint": adjoint, "cpu_baseline": cpu,
     }
     if rank == 0:

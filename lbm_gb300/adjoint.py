@@ -17,6 +17,12 @@ set_bc must give every wall a Zou-He operation and apply the four corners).
 
 Memory: T/K checkpoints + 2 K recomputed states + two adjoint states, i.e.
 about 3 sqrt(T) copies of the lattice instead of T.
+
+``DragObjective.apply(om_p, inlet, adjoint, T, window, weights)`` is the same
+objective as a ``torch.autograd.Function`` of the TRT rate and the inlet
+profile (the first ny entries of the BC vector: the x-velocity of the left
+wall per row, scaled by the inlet ramp): forward runs ``forward``, backward
+runs ``gradient``.
 """
 import ctypes
 import math
@@ -183,3 +189,42 @@ class DragAdjoint:
         return {"omega": g_om, "bc_vec": bufs["grad_bc_vec"].cpu().numpy(),
                 "bc_base": bufs["grad_bc_base"].cpu().numpy(),
                 "g0": lam[cur ^ 1].cpu().numpy().reshape(9, self.lat.nx, self.lat.ny)}
+
+
+class DragObjective(torch.autograd.Function):
+    """J(om_p, inlet) of a ``DragAdjoint`` as a differentiable torch op.
+
+    om_p: 0-d float64 tensor, the TRT rate om+ (om- follows, lambda = 1/4);
+    inlet: float64 tensor of ny entries, the inlet x-velocity profile (first
+    ny entries of the packed BC vector); T, window, weights as in
+    ``DragAdjoint.forward``.  Returns J as a 0-d float64 tensor on the
+    device of om_p; backward gives dJ/d om_p and dJ/d inlet from the
+    discrete adjoint (one adjoint sweep per backward)."""
+
+    @staticmethod
+    def forward(ctx, om_p, inlet, adjoint, T, window, weights):
+        ny = adjoint.lat.ny
+        prof = inlet.detach().to("cpu", torch.float64).numpy().reshape(-1)
+        if prof.size != ny:
+            raise ValueError("inlet profile has %d entries, the lattice has ny = %d"
+                             % (prof.size, ny))
+        if not hasattr(adjoint, "vec"):
+            base, vec, _ = adjoint.sched
+            adjoint.base, adjoint.vec = base.copy(), vec.copy()
+        vec = adjoint.vec.copy()
+        vec[:ny] = prof
+        adjoint.vec = vec
+        adjoint.set_omega(float(om_p))
+        J = adjoint.forward(T, window, weights)
+        ctx.adjoint = adjoint
+        ctx.devices = (om_p.device, inlet.device)
+        return torch.tensor(J, dtype=torch.float64, device=om_p.device)
+
+    @staticmethod
+    def backward(ctx, grad_J):
+        g = ctx.adjoint.gradient()
+        ny = ctx.adjoint.lat.ny
+        s = float(grad_J)
+        g_om = torch.tensor(s * g["omega"], dtype=torch.float64, device=ctx.devices[0])
+        g_in = torch.from_numpy(s * g["bc_vec"][:ny]).to(ctx.devices[1])
+        return g_om, g_in, None, None, None, None

@@ -340,7 +340,7 @@ __global__ void k_pack(const double* __restrict__ g, typename St::S* __restrict_
   const long long i = c / ny, s = i * sy + (c - i * ny);
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
-    const double v = g[q * n + c] - (St::kShift ? wgt(q) * rho0 : 0.0);
+    const double v = (g[q * n + c] - (St::kShift ? wgt(q) * rho0 : 0.0)) * (double)St::kScale;
     St::store(f + q * ns + s, (typename St::T)v);
   }
 }
@@ -353,7 +353,8 @@ __global__ void k_unpack(const typename St::S* __restrict__ f, double* __restric
   const long long i = c / ny, s = i * sy + (c - i * ny);
 #pragma unroll
   for (int q = 0; q < 9; ++q)
-    g[q * n + c] = (double)St::load(f + q * ns + s) + (St::kShift ? wgt(q) * rho0 : 0.0);
+    g[q * n + c] = (double)St::load(f + q * ns + s) * (double)St::kInvScale +
+                   (St::kShift ? wgt(q) * rho0 : 0.0);
 }
 
 int check_conv(const char* fn, const void* g, const void* f, int nx, int ny, int sy) {

@@ -44,16 +44,27 @@ __device__ __forceinline__ float recip(float x) { return 1.0f / x; }
 
 // ---------------------------------------------------------------------------
 // Storage forms.  Full-precision values are T (double for F64, float for the
-// reduced forms); shifted forms store d = f - w_q * rho0.
+// reduced forms); shifted forms store d = kScale (f - w_q * rho0).  FP16
+// stores the deviations times 2^10: FP16's normal range [2^-14, 65504] then
+// covers |f - w rho0| in [6e-8, 64], so the small deviations of a slowly
+// starting flow keep 11 significant bits instead of falling into FP16's
+// subnormals (and its overflow bound stays far above any deviation of a
+// stable lattice).  The scale is exact (a power of two) and folds into the
+// moments (moments(): rho = rho0 + drho / kScale, u = j / (kScale rho)); the
+// collision is linear in (d, drho, j) at fixed u.
 // ---------------------------------------------------------------------------
 // store_r(p, v, r): the store of a kernel's update, given 32 random bits r;
 // only the stochastic-rounding forms use r.
+#ifndef LBM_F16_SCALE_LOG2
+#define LBM_F16_SCALE_LOG2 10
+#endif
 struct StoreF64 {
   using S = double;
   using T = double;
   static constexpr bool kShift = false;
   static constexpr bool kFixed = false;
   static constexpr bool kStochastic = false;
+  static constexpr T kScale = 1, kInvScale = 1;
   __device__ static T load(const S* p) { return *p; }
   __device__ static void store(S* p, T v) { *p = v; }
   __device__ static void store_r(S* p, T v, unsigned) { *p = v; }
@@ -65,6 +76,7 @@ struct StoreF32 {
   static constexpr bool kShift = true;
   static constexpr bool kFixed = false;
   static constexpr bool kStochastic = false;
+  static constexpr T kScale = 1, kInvScale = 1;
   __device__ static T load(const S* p) { return *p; }
   __device__ static void store(S* p, T v) { *p = v; }
   __device__ static void store_r(S* p, T v, unsigned) { *p = v; }
@@ -76,6 +88,7 @@ struct StoreF16 {
   static constexpr bool kShift = true;
   static constexpr bool kFixed = false;
   static constexpr bool kStochastic = false;
+  static constexpr T kScale = (T)(1 << LBM_F16_SCALE_LOG2), kInvScale = T(1) / kScale;
   __device__ static T load(const S* p) { return __half2float(*p); }
   __device__ static void store(S* p, T v) { *p = __float2half_rn(v); }
   __device__ static void store_r(S* p, T v, unsigned) { *p = __float2half_rn(v); }
@@ -90,6 +103,7 @@ struct StoreBF16 {
   static constexpr bool kShift = true;
   static constexpr bool kFixed = false;
   static constexpr bool kStochastic = false;
+  static constexpr T kScale = 1, kInvScale = 1;
   __device__ static T load(const S* p) { return __bfloat162float(*p); }
   __device__ static void store(S* p, T v) { *p = __float2bfloat16_rn(v); }
   __device__ static void store_r(S* p, T v, unsigned) { *p = __float2bfloat16_rn(v); }
@@ -241,6 +255,7 @@ struct StoreQ60 {
   static constexpr bool kShift = false;
   static constexpr bool kFixed = true;
   static constexpr bool kStochastic = false;
+  static constexpr T kScale = 1, kInvScale = 1;
   __device__ static T load(const S* p) { return q60_to_double(*p); }
   __device__ static void store(S* p, T v) { *p = q60_from_double(v); }
   __device__ static void store_r(S* p, T v, unsigned) { *p = q60_from_double(v); }
@@ -411,15 +426,17 @@ struct Moments {
 };
 
 template <typename T, bool SHIFT>
-__device__ __forceinline__ Moments<T, SHIFT> moments(const T d[9], T rho0) {
+// inv_scale: 1 / the storage form's kScale (drho and j stay scaled, rho and
+// u are the physical values).
+__device__ __forceinline__ Moments<T, SHIFT> moments(const T d[9], T rho0, T inv_scale = T(1)) {
   Moments<T, SHIFT> m;
   T s12 = d[1] + d[2], s34 = d[3] + d[4], s56 = d[5] + d[6], s78 = d[7] + d[8];
   T d12 = d[1] - d[2], d34 = d[3] - d[4], d56 = d[5] - d[6], d87 = d[8] - d[7];
   m.drho = (((d[0] + s12) + s34) + s56) + s78;
-  m.rho = SHIFT ? rho0 + m.drho : m.drho;
+  m.rho = SHIFT ? rho0 + m.drho * inv_scale : m.drho;
   m.jx = (d12 + d56) + d87;
   m.jy = (d34 + d56) - d87;
-  T r = recip(m.rho);
+  T r = recip(m.rho) * inv_scale;
   m.ux = m.jx * r;
   m.uy = m.jy * r;
   return m;

@@ -177,7 +177,8 @@ __device__ __forceinline__ void bulk_cell(const FusedArgs& a, long long cell) {
     // Input is the full post-BC g (FP64) of every cell, edges included.
 #pragma unroll
     for (int q = 0; q < 9; ++q)
-      d[q] = St::kShift ? (T)(a.g_out[q * N + rc] - wgt(q) * a.kd.rho0) : (T)a.g_out[q * N + rc];
+      d[q] = St::kShift ? (T)(a.g_out[q * N + rc] - wgt(q) * a.kd.rho0) * St::kScale
+                        : (T)a.g_out[q * N + rc];
   } else {
     if (i == 0 || i == a.nx - 1 || j == 0 || j == a.ny - 1) return;
     const long long sy = a.sy;
@@ -192,11 +193,12 @@ __device__ __forceinline__ void bulk_cell(const FusedArgs& a, long long cell) {
     d[8] = St::load(fin + 8 * Ns + cell - sy + 1);
     if (MODE == LBM_MODE_FINISH) {
 #pragma unroll
-      for (int q = 0; q < 9; ++q) a.g_out[q * N + rc] = (double)(d[q] + (St::kShift ? k.w[q] : T(0)));
+      for (int q = 0; q < 9; ++q)
+        a.g_out[q * N + rc] = (double)(St::kShift ? d[q] * St::kInvScale + k.w[q] : d[q]);
       return;
     }
   }
-  Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+  Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0, St::kInvScale);
   if (a.write_macro) {
     a.rho_out[rc] = (double)m.rho;
     a.u_out[rc] = (double)m.ux;
@@ -298,7 +300,7 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
           d[q] = St::load(&in[q].v[c]);
         }
       }
-      Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+      Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0, St::kInvScale);
       const int j = j0 + c;
       if (j < ny && a.write_macro) {
         const long long rc = (long long)i * ny + j;
@@ -338,7 +340,7 @@ __device__ __forceinline__ typename St::T full_value(const typename St::S* p, in
                                                      typename St::T rho0) {
   using T = typename St::T;
   const T v = St::load(p);
-  return St::kShift ? v + T(wgt(q)) * rho0 : v;
+  return St::kShift ? v * St::kInvScale + T(wgt(q)) * rho0 : v;
 }
 
 // Resident 128-thread blocks per SM that the special-cell kernels are
@@ -577,8 +579,8 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
   double* mac_out = a.mac[it & 1];
   T d[9];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) d[q] = St::kShift ? c.g[q] - T(wgt(q)) * rho0 : c.g[q];
-  Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0);
+  for (int q = 0; q < 9; ++q) d[q] = St::kShift ? (c.g[q] - T(wgt(q)) * rho0) * St::kScale : c.g[q];
+  Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0, St::kInvScale);
   if (is_corner_neighbour(a, s)) {
     mac_out[s] = (double)m.rho;
     mac_out[a.n_special + s] = (double)m.ux;

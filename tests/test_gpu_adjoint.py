@@ -85,3 +85,18 @@ def test_adjoint_matches_central_differences(run):
         fd = (J_at(vec=vp) - J_at(vec=vm)) / (2 * h)
         assert abs(fd - grad["bc_vec"][j]) <= 1e-5 * abs(grad["bc_vec"][j]) + 1e-9
     J_at()
+
+
+def test_autograd_function_gives_the_adjoint_gradient(run):
+    from lbm_gb300.adjoint import DragObjective
+    app, lat, adj, J, grad, w = run
+    ny = lat.ny
+    base, vec, _ = adj.sched
+    om = torch.tensor(lat.om_p_lbm, dtype=torch.float64, requires_grad=True)
+    inlet = torch.tensor(vec[:ny], dtype=torch.float64, requires_grad=True)
+    Jt = DragObjective.apply(om, inlet, adj, T, WIN, w)
+    (2.0 * Jt).backward()
+    assert abs(Jt.item() - J) <= 1e-13 * abs(J)
+    assert abs(om.grad.item() - 2.0 * grad["omega"]) <= 1e-12 * abs(grad["omega"])
+    ref = 2.0 * grad["bc_vec"][:ny]
+    assert np.max(np.abs(inlet.grad.numpy() - ref)) <= 1e-12 * np.max(np.abs(ref))
