@@ -39,12 +39,15 @@ def test_every_declared_symbol_is_exported():
     assert sorted(set(names) - set(_lib.exported_symbols())) == []
 
 
-def test_problem_struct_layout_matches_c():
-    fields = [f[0] for f in _lib.Problem._fields_]
+@pytest.mark.parametrize("cls,cname", [(_lib.Problem, "lbm_problem"),
+                                        (_lib.BatchConfig, "lbm_batch_config"),
+                                        (_lib.Adjoint, "lbm_adjoint")])
+def test_struct_layout_matches_c(cls, cname):
+    fields = [f[0] for f in cls._fields_]
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "lbm_gb300.h"', "int main(void){"]
-    src.append('printf("size %zu\\n", sizeof(lbm_problem));')
+    src.append('printf("size %%zu\\n", sizeof(%s));' % cname)
     for f in fields:
-        src.append('printf("%s %%zu\\n", offsetof(lbm_problem, %s));' % (f, f))
+        src.append('printf("%s %%zu\\n", offsetof(%s, %s));' % (f, cname, f))
     src.append("return 0;}")
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "t.c")
@@ -53,9 +56,9 @@ def test_problem_struct_layout_matches_c():
         subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe])
         out = subprocess.check_output([exe]).decode().split("\n")
     got = dict(line.split() for line in out if line.strip())
-    assert int(got["size"]) == ctypes.sizeof(_lib.Problem)
+    assert int(got["size"]) == ctypes.sizeof(cls)
     for f in fields:
-        assert int(got[f]) == getattr(_lib.Problem, f).offset, f
+        assert int(got[f]) == getattr(cls, f).offset, f
 
 
 def test_scratch_bytes_is_host_only():
@@ -75,3 +78,21 @@ def test_argument_errors_are_reported_without_gpu_work():
     assert L.lbm_advance(ctypes.byref(P), 1, 0, 1, 0, 0, None) == _lib.LBM_ERR_ARG
     with pytest.raises(_lib.LbmError):
         _lib.call("lbm_zou_he_f64", 9, None, None, None, None, None, 8, 8, None)
+
+
+def test_batch_config_checked_without_gpu_work():
+    """A batch configuration outside its documented ranges (tile_rounds
+    1..64, vec_bytes 8 or 16, persistent 0 or 1) is refused by the host
+    checks of lbm_batch_create."""
+    L = _lib.load()
+    P = _lib.Problem()
+    good = dict(bulk_threads=128, bulk_blocks_per_sm=8, special_blocks_per_sm=8,
+                scalar_tile_cells=2048, persistent=0, vec_bytes=8, tile_rounds=4)
+    for key, bad in (("tile_rounds", 0), ("tile_rounds", 65), ("vec_bytes", 4),
+                     ("persistent", 2), ("bulk_threads", 48)):
+        cfg = _lib.BatchConfig(**dict(good, **{key: bad}))
+        h = ctypes.c_void_p()
+        rc = L.lbm_batch_create(ctypes.byref(h), ctypes.byref(P), 1, ctypes.byref(cfg))
+        assert rc == _lib.LBM_ERR_ARG, (key, bad)
+        assert b"bad config" in L.lbm_last_error_string()
+        assert not h.value
