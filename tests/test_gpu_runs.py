@@ -80,6 +80,46 @@ def test_config0_cavity200_vs_oracle(cuda, precision):
     assert max_rel(out["rho"], lat.rho) <= TOL
 
 
+def _tiny_cavity(n):
+    from lbm_gb300.apps import cavity
+    a = cavity()
+    a.L_lbm, a.u_lbm, a.Re_lbm = n, 0.1, 10.0
+    a.compute_lbm_parameters()
+    a.sigma = 20.0
+    a.stop, a.it_max, a.output_freq = "it", 199, 10 ** 12
+    return a
+
+
+@pytest.mark.parametrize("n", [4, 5, 7])
+def test_tiny_lattices(cuda, n):
+    """Smallest lattices: at n = 4 twelve of the sixteen cells are walls or
+    corners (the corners' x-neighbours are bottom/top wall cells), and the reduced
+    forms pad rows to 16 bytes (8 cells of FP16/BF16, 4 or 8 of FP32).  Plain
+    forms against the oracle
+    (<= 1e-12), reduced forms against the FP64 run."""
+    lat, _ = run_oracle(_tiny_cavity(n))
+    ref = None
+    for precision in PLAIN:
+        out, _, _ = run_gpu(_tiny_cavity(n), fused=True, precision=precision)
+        assert max_rel(out["g"], lat.g) <= TOL, precision
+        assert max_rel(out["g_up"], lat.g_up) <= TOL, precision
+        ref = out
+    for precision in ("f32", "f16sr", "bf16s"):
+        out, _, glat = run_gpu(_tiny_cavity(n), fused=True, precision=precision)
+        v = 4 if precision == "f32" else 8  # 16-byte rows
+        assert glat._engine.sy == -(-n // v) * v
+        assert np.all(np.isfinite(out["g"]))
+        assert np.max(np.abs(out["u"] - ref["u"])) <= 2e-2 * np.max(np.abs(ref["u"]))
+
+
+def test_lattice_below_minimum_is_refused(cuda):
+    """A 3 x 3 lattice is below the fused engine's minimum (4 x 4): the host
+    checks refuse it before any kernel runs."""
+    from lbm_gb300._lib import LbmError
+    with pytest.raises(LbmError, match="outside"):
+        run_gpu(_tiny_cavity(3), fused=True, precision="f64")
+
+
 def test_reference_cavity_known_values(cuda):
     """lbm/tst/cavity/test_cavity.py: default cavity, 4 centre-line values to 1e-6."""
     from lbm_gb300.apps import cavity
