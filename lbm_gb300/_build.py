@@ -1,14 +1,19 @@
 """Build liblbm_gb300.so (sm_103a) in-tree with nvcc.
 
-Three translation units are compiled in parallel and linked with the static
+Five translation units are compiled in parallel and linked with the static
 CUDA runtime:
 
 * ``lbm_fused.cu``   fused pull-scheme engine (all storage forms)
 * ``lbm_unfused.cu`` one kernel per reference function, ``-fmad=false``
 * ``lbm_api.cu``     C-ABI front, CUDA-graph cache, storage conversion
-* ``lbm_batch.cu``   batched lattices (persistent work-queue kernels)
+* ``lbm_batch.cu``   batched lattices (work-queue and per-tile kernels)
+* ``lbm_adjoint.cu`` discrete adjoint of the FP64 fused step
+
+Processes that build at the same time (one per rank under torchrun) take
+turns on a lock file; each rebuilds only if the library is still stale.
 """
 import concurrent.futures
+import fcntl
 import os
 import shutil
 import subprocess
@@ -55,6 +60,17 @@ def build(force=False, verbose=False, extra=()):
     if not force and up_to_date():
         return LIB_PATH
     os.makedirs(OBJ_DIR, exist_ok=True)
+    with open(os.path.join(OBJ_DIR, "build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            if not force and up_to_date():  # built by another process meanwhile
+                return LIB_PATH
+            return _compile_and_link(verbose, extra)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _compile_and_link(verbose, extra):
     nv = nvcc()
 
     def compile_unit(item):
