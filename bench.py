@@ -22,10 +22,13 @@ HBM copy bandwidth; ``forms`` are the other storage forms on the same
 workload (``f64``: FP64 storage and arithmetic, bounded by the FP64 pipe,
 reported with that second bound); ``form_errors`` runs the cylinder channel
 (ny 200, nx 1100, Re 100) in every form and states the error of each against
-the FP64 run; ``batched_sweep`` is the 256-case sweep; ``adjoint`` is the
-drag-gradient cost on the ny 100 channel; ``cpu_baseline`` is the C
-restatement of the reference kernels (oracle/, OpenMP over all host cores) on
-a bounded sample of the same workload.
+the FP64 run; ``array_form_errors`` (``--array-errors N``, off by default)
+does the same on this workload for N iterations; ``batched_sweep`` is the
+256-case sweep; ``adjoint`` is the drag-gradient cost on the ny 100 channel;
+``cpu_baseline`` is the C restatement of the reference kernels (oracle/,
+OpenMP over all host cores) on a bounded sample of the same workload.
+Under torchrun (N > 1) every rank runs one independent replica; the whole-job
+figures are the slowest rank's (replica_totals).
 """
 import argparse
 import contextlib
