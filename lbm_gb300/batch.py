@@ -21,7 +21,6 @@ import io
 import itertools
 import math
 import tempfile
-import time
 
 import numpy as np
 import torch
