@@ -20,6 +20,9 @@ Outputs (``*.npz``, float64 / int64):
   per-step drag/lift, and for obstacle apps the link list and IBB distances.
 * ``geometry.npz`` -- polygons from ``generate_shape`` and link lists from
   ``lattice.add_obstacle`` (turek at L=24/100/200, squares).
+* ``buff.npz`` -- the reference observable buffer (``lbm/src/utils/buff.py``)
+  fed a seeded decaying oscillation: ``mv_avg`` output and the convergence
+  flag at every iteration, and the final history arrays.
 
 The GPU machine does not hold the reference; only these files travel.
 Run: ``python tests/golden/make_golden.py --reference <path-to-lbm-checkout>``.
@@ -238,18 +241,50 @@ def make_geometry(R, out):
     np.savez_compressed(out, **res)
 
 
+def buff_series(n=3000, seed=5):
+    """Seeded observable history fed to the buffer (also used by the test)."""
+    rng = np.random.default_rng(seed)
+    it = np.arange(n)
+    return 3.0 + 0.5 * np.exp(-it / 400.0) * np.sin(it / 15.0) + 1e-3 * rng.standard_normal(n)
+
+
+BUFF_ARGS = dict(dt=0.01, obs_cv_ct=1e-2, obs_cv_nb=100)
+
+
+def make_buff(out):
+    from lbm.src.utils.buff import buff
+    b = buff("drag", BUFF_ARGS["dt"], BUFF_ARGS["obs_cv_ct"], BUFF_ARGS["obs_cv_nb"], ".")
+    obs, growth, cv = [], [], []
+    for v in buff_series():
+        b.add(v)
+        o, g = b.mv_avg()
+        obs.append(o)
+        growth.append(g)
+        cv.append(int(b.obs_cv))
+    np.savez_compressed(out, obs=np.array(obs), growth=np.array(growth), cv=np.array(cv),
+                        buff=b.buff, avg1=b.avg1_buff, avg2=b.avg2_buff, avg3=b.avg3_buff,
+                        f_avg=b.f_avg())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("LBM_REFERENCE"))
+    ap.add_argument("--only", choices=["kernels", "geometry", "runs", "buff"], default=None)
     args = ap.parse_args()
     if not args.reference or not os.path.isdir(args.reference):
         sys.exit("pass --reference <path to the jviquerat/lbm checkout>")
     R = _import_reference(os.path.abspath(args.reference))
-    make_fn_kernels(R, os.path.join(HERE, "fn_kernels.npz"))
-    print("fn_kernels.npz written")
-    make_geometry(R, os.path.join(HERE, "geometry.npz"))
-    print("geometry.npz written")
-    make_runs(R)
+    if args.only in (None, "kernels"):
+        make_fn_kernels(R, os.path.join(HERE, "fn_kernels.npz"))
+        print("fn_kernels.npz written")
+    if args.only in (None, "geometry"):
+        make_geometry(R, os.path.join(HERE, "geometry.npz"))
+        print("geometry.npz written")
+    if args.only in (None, "runs"):
+        make_runs(R)
+    if args.only in (None, "buff"):
+        make_buff(os.path.join(HERE, "buff.npz"))
+        print("buff.npz written")
 
 
 if __name__ == "__main__":
