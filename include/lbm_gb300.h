@@ -97,9 +97,10 @@ int lbm_bounce_back_f64(int ibb, const int32_t* links, int64_t n, const double* 
 size_t lbm_drag_lift_scratch_bytes(int64_t n);
 int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* g_up, const double* g,
                       int nx, int ny, double* out, void* scratch, void* stream);
-/* Same result as lbm_drag_lift_f64, for callers that cannot provide device
- * memory (their device memory belongs to another allocator, or they must not
- * allocate after start-up).  No counterpart in the reference.  The block
+/* Same result as lbm_drag_lift_f64 (nb_drag_lift, nb.py:49-73), for callers
+ * that cannot provide device memory (their device memory belongs to another
+ * allocator, or they must not allocate after start-up); the scratch-free
+ * calling form has no counterpart in the reference.  The block
  * partials live in a fixed 64 KiB array inside the library's device image,
  * held by every GPU that loads the library until exit; at most
  * LBM_DRAG_NOALLOC_MAX_LINKS links per call (more: LBM_ERR_ARG).  The first
@@ -211,7 +212,11 @@ typedef struct lbm_problem {
 #define LBM_FLAG_WALL_MACRO 4u   /* FINISH: write rho/u written by wall ops      */
 
 size_t lbm_problem_scratch_bytes(const lbm_problem* p);
-/* Advance n_steps iterations.  it0 is the reference iteration number of the
+/* Advance n_steps iterations: each is one pass of the reference's run() loop
+ * body (run.py:24-54: lattice.macro, equilibrium, collision_stream, then the
+ * app's set_bc -- bounce_back_obstacle, zou_he_* walls and corners -- and
+ * the drag_lift observable; nb.py:7-344), fused into three kernels.  it0 is
+ * the reference iteration number of the
  * first collision performed by this call (its BCs use iteration it0 - 1 and
  * its drag output lands in drag_hist[(it0 - 1) % drag_cap]).  parity selects
  * which of f[0]/f[1] holds the input.  mode: LBM_MODE_*.  For
@@ -224,8 +229,9 @@ int lbm_advance(const lbm_problem* p, int mode, int64_t it0, int n_steps, int pa
  * parity); a graph is re-captured when the problem descriptor changes). */
 int lbm_advance_graph(const lbm_problem* p, int64_t it0, int n_steps, int parity,
                       uint32_t flags, void* stream);
-/* Per-kernel timing: runs n_steps LBM_MODE_STEP iterations (no graph) with
- * CUDA events around each kernel and synchronises.  ms_out[0..2] = average
+/* Per-kernel timing (measurement helper, no counterpart in the reference):
+ * runs n_steps LBM_MODE_STEP iterations (no graph) with CUDA events around
+ * each kernel and synchronises.  ms_out[0..2] = average
  * milliseconds of the bulk, special-cell and drag kernels per step,
  * ms_out[3] = kernels launched per step. */
 int lbm_profile_steps(const lbm_problem* p, int64_t it0, int n_steps, int parity, uint32_t flags,
@@ -324,8 +330,9 @@ int lbm_adjoint_sweep(const lbm_problem* p, const lbm_adjoint* adj, int64_t it_f
 int lbm_adjoint_initial(const lbm_problem* p, const lbm_adjoint* adj, const double* g0,
                         const double* lam_in, double* lam_out, void* stream);
 
-/* Convert distributions between the FP64 reference layout and a storage form
- * (shifted forms store f - w_q * rho0).  g has rows of ny, f rows of
+/* Convert distributions between the FP64 reference layout (lattice.g,
+ * float64 [9][nx][ny], lattice.py:155-157) and a storage form (shifted forms
+ * store kScale (f - w_q * rho0), kScale = 2^10 for FP16, 1 otherwise).  g has rows of ny, f rows of
  * row_pitch (0 = ny); padding elements of f are left untouched. */
 int lbm_pack_f64(int precision, const double* g, void* f, int nx, int ny, int row_pitch, double rho0,
                  void* stream);
