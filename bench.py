@@ -607,7 +607,7 @@ def main():
 
     import torch
     import __graft_entry__
-    __graft_entry__.build()
+    __graft_entry__.build(verbose=False)
     dist = None
     if world > 1:
         import torch.distributed as dist

@@ -34,7 +34,7 @@ extern "C" {
 
 /* ---- enums ---------------------------------------------------------------- */
 /* Storage/compute forms of the fused engine. */
-#define LBM_PREC_F64 0   /* FP64 storage, FP64 arithmetic (the plain path)          */
+#define LBM_PREC_F64 0   /* FP64 storage, FP64 arithmetic                           */
 #define LBM_PREC_F32 1   /* FP32 storage of f - w*rho0, FP32 arithmetic              */
 #define LBM_PREC_F16S 2  /* FP16 storage of f - w*rho0, FP32 arithmetic              */
 #define LBM_PREC_BF16S 3 /* BF16 storage of f - w*rho0, FP32 arithmetic              */
@@ -97,18 +97,17 @@ int lbm_bounce_back_f64(int ibb, const int32_t* links, int64_t n, const double* 
 size_t lbm_drag_lift_scratch_bytes(int64_t n);
 int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* g_up, const double* g,
                       int nx, int ny, double* out, void* scratch, void* stream);
-/* Same result as lbm_drag_lift_f64 (nb_drag_lift, nb.py:49-73), for callers
- * that cannot provide device memory (their device memory belongs to another
- * allocator, or they must not allocate after start-up); the scratch-free
- * calling form has no counterpart in the reference.  The block
+/* Same result as lbm_drag_lift_f64, for callers that cannot provide device
+ * memory (their device memory belongs to another allocator, or they must not
+ * allocate after start-up).  No counterpart in the reference.  The block
  * partials live in a fixed 64 KiB array inside the library's device image,
  * held by every GPU that loads the library until exit; at most
  * LBM_DRAG_NOALLOC_MAX_LINKS links per call (more: LBM_ERR_ARG).  The first
- * call on each device looks up the array's device address (with that device
- * current); make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU (different streams, or
- * different host threads) race and must be serialised by the caller.
- * Allocates nothing. */
+ * call in each CUDA context (the device's primary context, or a context the
+ * host made current) looks up the array's device address in that context;
+ * make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (different streams, or different host
+ * threads) race and must be serialised by the caller.  Allocates nothing. */
 #define LBM_DRAG_NOALLOC_MAX_LINKS 1048576
 int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const double* g_up,
                               const double* g, int nx, int ny, double* out, void* stream);

@@ -56,7 +56,8 @@ def up_to_date():
 
 
 def build(force=False, verbose=False, extra=()):
-    """Compile and link; returns the library path."""
+    """Compile and link; returns the library path.  verbose: print every
+    nvcc command line (and anything nvcc prints) to stdout."""
     if not force and up_to_date():
         return LIB_PATH
     os.makedirs(OBJ_DIR, exist_ok=True)
@@ -90,6 +91,8 @@ def _compile_and_link(verbose, extra):
         objs = list(ex.map(compile_unit, UNITS.items()))
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     cmd = [nv, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    if verbose:
+        print(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

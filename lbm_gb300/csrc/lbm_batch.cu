@@ -121,7 +121,9 @@ __global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_batch_special(c
                                                        const int4* __restrict__ tiles, int n_tiles,
                                                        unsigned* queue, long long* it_dev,
                                                        int last) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;  // next iteration's bulk queue
+  // The next iteration's bulk queue (lbm_batch_create refuses the persistent
+  // schedule for a batch without special tiles, where nothing would reset it).
+  if (blockIdx.x == 0 && threadIdx.x == 0) queue[0] = 0;
   __shared__ int t_sh;
   if (threadIdx.x == 0) t_sh = (int)atomicAdd(&queue[1], 1u);
   __syncthreads();
@@ -297,6 +299,14 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       special.push_back(make_int4(c, s, std::min(128, p.n_special - s), 0));
     if (p.drag_hist && p.n_links > 0)
       for (int o = 0; o < p.n_obstacles; ++o) drag.push_back(make_int2(c, o));
+  }
+  // The persistent bulk kernel's tile queue (queue[0]) is reset for the next
+  // iteration by the special-cell kernel, so that schedule needs special
+  // tiles.  Every lattice has them today (problem_check asks for at least the
+  // wall cells), and this check keeps that dependency explicit.
+  if (cfg->persistent && special.empty()) {
+    set_error("lbm_batch_create: the persistent schedule needs special cells in some lattice");
+    return LBM_ERR_ARG;
   }
   lbm_batch* b = new lbm_batch();
   b->n_cases = n_cases;

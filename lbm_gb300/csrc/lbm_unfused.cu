@@ -5,6 +5,8 @@
 // result.  This translation unit is compiled with -fmad=false: every product
 // and sum is rounded on its own as in NumPy, so the results equal the CPU
 // restatement bit for bit (division and square root are IEEE in both).
+#include <cuda.h>
+
 #include <mutex>
 
 #include "lbm_device.cuh"
@@ -332,13 +334,57 @@ extern "C" int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* 
 // the library's device image: every GPU that loads the library holds its
 // 64 KiB until the process exits.  The host must not pass the symbol itself
 // to a kernel (on the host it names a stand-in, not device memory); its
-// device address is fetched once per device with cudaGetSymbolAddress.
+// device address is fetched with cudaGetSymbolAddress once per CUDA context
+// (each context that loads the library has its own copy of the array).
 #define LBM_NOALLOC_MAX_BLOCKS (LBM_DRAG_NOALLOC_MAX_LINKS / 256)
 static __device__ __align__(256) double g_drag_noalloc_part[2 * LBM_NOALLOC_MAX_BLOCKS];
 
 namespace {
+// Contexts are told apart by the driver's context id (cuCtxGetId), which is
+// unique for the life of the process: a context destroyed and re-created
+// (cudaDeviceReset, or a host that makes its own driver context current)
+// gets a new id and a fresh look-up.  The driver entry points come through
+// the runtime, so the library does not link libcuda.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+struct NoallocEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
 std::mutex g_noalloc_mu;
-double* g_noalloc_addr[64] = {};
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+NoallocEntry g_noalloc_cache[64];
+int g_noalloc_n = 0;
+
+// Id of the calling thread's current context (made current by the runtime
+// if none is); false if the driver cannot tell.
+bool current_context_id(unsigned long long* id) {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) !=
+            cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) !=
+            cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return false;
+    g_ctx_get_current = (CtxGetCurrentFn)f1;
+    g_ctx_get_id = (CtxGetIdFn)f2;
+  }
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return false;
+  if (!ctx) {
+    // No context on this thread yet: bind the current device's primary
+    // context, as the runtime's first call on the thread would.
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return false;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  }
+  return g_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
 }  // namespace
 
 extern "C" int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const double* g_up,
@@ -355,25 +401,28 @@ extern "C" int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const 
               (long long)n, (int)LBM_DRAG_NOALLOC_MAX_LINKS);
     return LBM_ERR_ARG;
   }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    set_error("lbm_drag_lift_f64_noalloc: no usable current device");
-    return LBM_ERR_CUDA;
-  }
   double* part = nullptr;
   {
-    // One-time set-up per device, with that device current.
+    // One-time set-up per context, with that context current.
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    unsigned long long ctx_id = 0;
+    if (!current_context_id(&ctx_id)) {
+      set_error("lbm_drag_lift_f64_noalloc: no usable current CUDA context");
+      return LBM_ERR_CUDA;
+    }
+    for (int k = 0; k < g_noalloc_n; ++k)
+      if (g_noalloc_cache[k].ctx_id == ctx_id) part = g_noalloc_cache[k].addr;
+    if (!part) {
       void* addr = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&addr, g_drag_noalloc_part);
       if (e != cudaSuccess || !addr) {
         set_error("lbm_drag_lift_f64_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
         return LBM_ERR_CUDA;
       }
-      g_noalloc_addr[dev] = (double*)addr;
+      part = (double*)addr;
+      // A full table keeps its entries; later contexts look the address up on every call.
+      if (g_noalloc_n < 64) g_noalloc_cache[g_noalloc_n++] = NoallocEntry{ctx_id, part};
     }
-    part = g_noalloc_addr[dev];
   }
   // k_drag_partial writes all nb partials before k_drag_final reads them
   // (same stream), so nothing from the previous call has to be cleared.

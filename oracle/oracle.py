@@ -36,16 +36,20 @@ W = np.array([4. / 9.] + [1. / 9.] * 4 + [1. / 36.] * 4)
 _lib = None
 
 
-def build(force=False):
-    """Compile lbm_oracle.c with gcc (no FP contraction, so x86 == Arm)."""
+def build(force=False, verbose=False):
+    """Compile lbm_oracle.c with gcc (no FP contraction, so x86 == Arm);
+    verbose: print the gcc command line."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     src = os.path.join(HERE, "lbm_oracle.c")
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
         return LIB_PATH
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-                           "-fno-fast-math", "-fopenmp", "-o", tmp, src])
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
+           "-o", tmp, src]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

@@ -3,10 +3,11 @@
 The no-allocation variant exists for callers that cannot give the library
 device memory -- their device memory belongs to another allocator, or they
 must not allocate once set up.  It keeps its reduction partials in a fixed
-array inside the library, so this test checks, through the C-ABI, that two
-calls in a row (different inputs, the second reusing what the first left in
-the shared array) give the same drag/lift as the entry point that takes a
-caller buffer, and that a link count above the fixed limit is refused.
+array inside the library, so this test checks, through the C-ABI, that
+calls in a row (different inputs, each reusing what the one before left in
+the shared array; the first at exactly the fixed limit) give the same
+drag/lift as the entry point that takes a caller buffer, and that a link
+count above the fixed limit is refused.
 
 This file is collected last on purpose; it must pass alone in a fresh
 process as well as after the other tests.
@@ -57,9 +58,12 @@ def test_no_alloc_matches_buffered_entry_point_twice():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    # First call: many links (many partial blocks); second: fewer links, so a
-    # stale partial from the first call would change the sum if it were read.
-    for (nx, ny, n, seed) in ((300, 200, 200_000, 1), (64, 48, 3_000, 2)):
+    # First call: exactly the limit, so every slot of the fixed array (the
+    # last one included) is written and the size check's boundary is run;
+    # then fewer links each time, so a stale partial left by the call before
+    # would change the sum if it were read.
+    for (nx, ny, n, seed) in ((300, 200, MAX_LINKS, 3), (300, 200, 200_000, 1),
+                              (64, 48, 3_000, 2)):
         g, g_up, links = _inputs(nx, ny, n, seed)
         ref = _with_buffer(links, n, g_up, g, nx, ny, stream)
         got = _no_alloc(links, n, g_up, g, nx, ny, stream)
