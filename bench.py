@@ -23,10 +23,14 @@ workload (``f64``: FP64 storage and arithmetic, bounded by the FP64 pipe,
 reported with that second bound); ``form_errors`` runs the cylinder channel
 (ny 200, nx 1100, Re 100) in every form and states the error of each against
 the FP64 run; ``array_form_errors`` (``--array-errors N``, off by default)
-does the same on this workload for N iterations; ``batched_sweep`` is the
+does the same on this workload for N iterations; ``plain_vs_oracle`` checks
+the plain forms' Cd/Cl series over the whole channel run against the C
+oracle (run in a child process on the host cores meanwhile: the oracle is
+the checker there, never the thing measured); ``batched_sweep`` is the
 256-case sweep; ``adjoint`` is the drag-gradient cost on the ny 100 channel;
-``cpu_baseline`` is the C restatement of the reference kernels (oracle/,
-OpenMP over all host cores) on a bounded sample of the same workload.
+``cpu_baseline`` is the C restatement of the reference kernels driven by the
+reference loop in C (oracle/, OpenMP over the host cores) on a bounded
+sample of the same workload.
 Under torchrun (N > 1) every rank runs one independent replica; the whole-job
 figures are the slowest rank's (replica_totals).
 """
@@ -87,6 +91,8 @@ def parse():
     ap.add_argument("--sweep-steps", type=int, default=10000,
                     help="iterations of the 256-case batched sweep (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain-oracle", action="store_true",
+                    help="skip the oracle run of the channel behind plain_vs_oracle")
     ap.add_argument("--array-errors", type=int, default=0,
                     help="iterations of the obstacle-array workload in every form, errors "
                          "against FP64 (0: skipped; 100000 takes ~7 minutes)")
@@ -422,7 +428,8 @@ def measure_array_errors(steps, forms, tmp, ny):
 def measure_form_errors(steps, forms, tmp, ny=200):
     """Every form on the cylinder channel, errors stated against the FP64 run:
     velocity-field L2 at the last iteration, and mean Cd / rms Cl / max Cd /
-    max Cl over the second half of the run."""
+    max Cl over the second half of the run.  Also returns the Cd/Cl series
+    and final velocity of the two plain forms (f64, q60) for plain_vs_oracle."""
     import torch
     ref = run_channel("f64", ny, steps, tmp)
     half = slice(len(ref["cd"]) // 2, None)
@@ -436,10 +443,13 @@ def measure_form_errors(steps, forms, tmp, ny=200):
     out = {"case": "cylinder channel %dx%d, D = %d, Re 100, %d iterations (all forms from the "
                    "same initial state)" % (ref["nx"], ref["ny"], channel_app(ny, 2).D_lbm, steps),
            "f64": dict(sref, mlups=ref["mlups"])}
+    plain = {"f64": {k: ref[k] for k in ("cd", "cl", "u")}}
     for form in forms:
         if form == "f64":
             continue
         r = run_channel(form, ny, steps, tmp)
+        if form == "q60":
+            plain["q60"] = {k: r[k] for k in ("cd", "cl", "u")}
         st = stats(r)
         err = {k + "_rel": abs(st[k] - sref[k]) / abs(sref[k]) for k in sref}
         err["u_l2_rel"] = float(np.linalg.norm(r["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
@@ -448,7 +458,7 @@ def measure_form_errors(steps, forms, tmp, ny=200):
         out[form] = dict(st, mlups=r["mlups"], error_vs_f64=err)
         del r
         torch.cuda.empty_cache()
-    return out
+    return out, plain
 
 
 def measure_adjoint(steps, tmp, ny=100):
@@ -535,7 +545,10 @@ def fp64_bound(res):
 # ---------------------------------------------------------------------------
 # CPU arm (oracle port, all host threads)
 # ---------------------------------------------------------------------------
-def cpu_reference(ny, seconds, min_iters=2):
+def _oracle_lattice(app, td):
+    """The oracle's lattice with links from the vectorised builder (the cell
+    loops take hours at these sizes; the builder is pinned to them by the
+    geometry tests)."""
     from lbm_gb300 import geometry
     from oracle import oracle as O
 
@@ -543,31 +556,99 @@ def cpu_reference(ny, seconds, min_iters=2):
         def add_obstacle(self, obstacle):
             return geometry.add_obstacle(self, obstacle.polygon, obstacle.tag, self.IBB)
 
+    return _Lat(app, output_dir=os.path.join(td, ""))
+
+
+def cpu_reference(ny, seconds):
+    """The oracle port on the host cores: the reference loop (run.py:24-54)
+    in C with OpenMP cell loops, over a bounded sample of the workload."""
+    from oracle import oracle as O
     app = make_app(ny)
     with tempfile.TemporaryDirectory() as td, contextlib.redirect_stdout(io.StringIO()):
-        lat = _Lat(app, output_dir=os.path.join(td, ""))
+        lat = _oracle_lattice(app, td)
+        base, vec, scale = app.bc_schedule(lat)
         app.initialize(lat)
-        app.set_inlets(lat, 0)
-        # one untimed iteration, then a bounded sample
-        def iteration(it):
-            app.set_inlets(lat, it)
-            lat.macro()
-            lat.equilibrium()
-            lat.collision_stream()
-            app.set_bc(lat)
-            app.observables(lat, it)
-        iteration(0)
+        # two untimed iterations (the first touches the work arrays), then a
+        # bounded sample sized from the second
+        O.run_program(lat, app, 1, (base, vec, scale([0])), initialize=False)
         t0 = time.perf_counter()
-        n = 0
-        while n < min_iters or time.perf_counter() - t0 < seconds:
-            iteration(1 + n)
-            n += 1
+        O.run_program(lat, app, 1, (base, vec, scale([1])), initialize=False)
+        n = max(2, int(seconds / max(time.perf_counter() - t0, 1e-3)))
+        t0 = time.perf_counter()
+        O.run_program(lat, app, n, (base, vec, scale(np.arange(2, n + 2))), initialize=False)
         dt = time.perf_counter() - t0
     cells = lat.nx * lat.ny
     return {"value": cells * n / dt / 1e6, "unit": "MLUPS", "cores": O.threads(),
             "kind": "port",
             "sample": "%d iterations of the full %dx%d workload (FP64, C restatement of "
-                      "nb.py with OpenMP cell loops), %.1f s" % (n, lat.nx, lat.ny, dt)}
+                      "nb.py driven by the run.py loop in C, OpenMP cell loops), %.1f s"
+                      % (n, lat.nx, lat.ny, dt)}
+
+
+def _oracle_channel_series(ny, steps, path, threads):
+    """Child process of the plain_vs_oracle check: the cylinder channel on
+    the oracle for `steps` iterations; writes the Cd/Cl series (same
+    normalisation as run_channel) and the final interior velocity."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as O
+    app = channel_app(ny, steps)
+    with tempfile.TemporaryDirectory() as td, contextlib.redirect_stdout(io.StringIO()):
+        lat = _oracle_lattice(app, td)
+        base, vec, scale = app.bc_schedule(lat)
+        t0 = time.perf_counter()
+        raw = O.run_program(lat, app, steps, (base, vec, scale(np.arange(steps))))
+        dt = time.perf_counter() - t0
+    norm = -2.0 / (app.rho_lbm * app.D_lbm * app.u_avg ** 2)
+    np.savez(path, cd=raw[:, 0, 0] * norm, cl=raw[:, 0, 1] * norm, u=lat.u[:, 1:-1, 1:-1],
+             seconds=dt, threads=O.threads())
+
+
+def start_oracle_channel(ny, steps, tmp):
+    """Start the oracle run of the channel in a spawned process, leaving a
+    few host cores to the GPU measurements that run meanwhile."""
+    import multiprocessing
+    threads = max(1, (os.cpu_count() or 4) - 4)
+    path = os.path.join(tmp, "oracle_channel_%d.npz" % steps)
+    proc = multiprocessing.get_context("spawn").Process(
+        target=_oracle_channel_series, args=(ny, steps, path, threads))
+    proc.start()
+    return proc, path
+
+
+def plain_vs_oracle(proc, path, series, steps, ny):
+    """Cd/Cl series of the plain forms over the whole channel run against
+    the oracle: max deviation over the run relative to the series' maximum
+    magnitude, the first iteration where it exceeds 1e-12 of that maximum,
+    the relative error of mean Cd and rms Cl over the second half, and the
+    final interior velocity field."""
+    proc.join()
+    if proc.exitcode != 0 or not os.path.exists(path):
+        return {"error": "oracle run failed (exit code %s)" % proc.exitcode}
+    d = np.load(path)
+    out = {"case": "cylinder channel %dx%d, D = %d, Re 100, %d iterations, Cd/Cl of iterations "
+                   "0..%d" % (int(5.5 * ny), ny, channel_app(ny, 2).D_lbm, steps, steps - 2),
+           "oracle": {"seconds": float(d["seconds"]), "threads": int(d["threads"]),
+                      "kind": "C restatement of nb.py driven by the run.py loop (oracle/)"}}
+    half = slice((steps - 1) // 2, None)
+    for form, r in series.items():
+        res = {}
+        for k in ("cd", "cl"):
+            ref = d[k][:steps - 1]
+            got = r[k]
+            dev = np.abs(got - ref)
+            scale_ = np.max(np.abs(ref))
+            over = np.nonzero(dev > 1e-12 * scale_)[0]
+            res[k + "_series_max_rel"] = float(dev.max() / scale_)
+            res[k + "_first_it_above_1e-12"] = int(over[0]) if len(over) else None
+        cd_r, cl_r = d["cd"][:steps - 1][half], d["cl"][:steps - 1][half]
+        cd_g, cl_g = r["cd"][half], r["cl"][half]
+        res["cd_mean_rel"] = float(abs(cd_g.mean() - cd_r.mean()) / abs(cd_r.mean()))
+        rms = lambda x: float(np.sqrt((x ** 2).mean()))
+        res["cl_rms_rel"] = abs(rms(cl_g) - rms(cl_r)) / rms(cl_r)
+        u_in = r["u"][:, 1:-1, 1:-1]
+        res["u_interior_max_rel"] = float(np.max(np.abs(u_in - d["u"])) / np.max(np.abs(d["u"])))
+        out[form] = res
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -655,9 +736,15 @@ def main():
         for f in forms.values():
             f["x_vs_f64"] = f["mlups"] / ref64
 
-    form_errors = None
+    # The oracle's run of the channel (plain_vs_oracle) goes on on the host
+    # cores while the GPU measurements below run.
+    oracle_job = None
+    if rank == 0 and world == 1 and args.error_steps > 0 and not args.no_plain_oracle:
+        oracle_job = start_oracle_channel(200, args.error_steps, tmp)
+
+    form_errors = plain_series = None
     if rank == 0 and args.error_steps > 0:
-        form_errors = measure_form_errors(args.error_steps, FORMS, tmp)
+        form_errors, plain_series = measure_form_errors(args.error_steps, FORMS, tmp)
         torch.cuda.empty_cache()
 
     array_errors = None
@@ -674,6 +761,10 @@ def main():
     if rank == 0 and args.adjoint_steps > 0:
         adjoint = measure_adjoint(args.adjoint_steps, tmp)
         torch.cuda.empty_cache()
+
+    plain_oracle = None
+    if oracle_job is not None:
+        plain_oracle = plain_vs_oracle(*oracle_job, plain_series, args.error_steps, 200)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -701,6 +792,7 @@ def main():
         "kernel_ms": res["kernel_ms"], "e2e": e2e,
         "gpu_launches": args.steps * res["kernels_per_step"],
         "clocks": clocks, "forms": forms, "form_errors": form_errors,
+        "plain_vs_oracle": plain_oracle,
         "array_form_errors": array_errors,
         "batched_sweep": sweep, "adjoint": adjoint, "cpu_baseline": cpu,
     }

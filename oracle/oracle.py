@@ -45,7 +45,7 @@ def build(force=False, verbose=False):
             and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
         return LIB_PATH
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
+    cmd = ["gcc", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
            "-o", tmp, src]
     if verbose:
         print(" ".join(cmd))
@@ -76,12 +76,14 @@ def lib():
             "oracle_zh_bottom": [dp, dp, dp, dp, i, i],
             "oracle_corner": [i, dp, dp, dp, i, i],
             "oracle_threads": [],
+            "oracle_run": [dp] * 10 + [i, i, d, d, i, ctypes.POINTER(ctypes.c_int32), i, lp, lp,
+                                       dp, i, dp, dp, dp, ctypes.c_int64, dp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = i if name in ("oracle_drag_lift", "oracle_bounce_back",
-                                       "oracle_threads") else None
+                                       "oracle_threads", "oracle_run") else None
         _lib = L
     return _lib
 
@@ -351,6 +353,83 @@ class OracleLattice:
 
     def generate_image(self, obstacles):
         pass
+
+
+_WALLS = {"zou_he_left_wall_velocity": 0, "zou_he_right_wall_velocity": 1,
+          "zou_he_right_wall_pressure": 2, "zou_he_top_wall_velocity": 3,
+          "zou_he_bottom_wall_velocity": 4}
+
+
+class _Program:
+    """Records the lattice calls of an app's set_bc as (kind, arg) pairs:
+    0 = bounce-back of obstacle arg, 1 = Zou-He wall, 2 = corner."""
+
+    def __init__(self, obstacles):
+        self.obstacles = list(obstacles)
+        self.ops = []
+
+    def bounce_back_obstacle(self, obs):
+        self.ops.append((0, next(k for k, o in enumerate(self.obstacles) if o is obs)))
+
+    def __getattr__(self, name):
+        if name in _WALLS:
+            return lambda: self.ops.append((1, _WALLS[name]))
+        if name.startswith("zou_he_") and name.endswith("_corner"):
+            return lambda: self.ops.append((2, CORNERS[name[len("zou_he_"):-len("_corner")]]))
+        raise AttributeError(name)
+
+
+def run_program(lat, app, n_iter, schedule, initialize=True):
+    """Iterations of ``run`` (below) in one C call (oracle_run): the same
+    kernels in the same order, for an app whose ``outputs`` does nothing in
+    those iterations and whose ``set_inlets(lat, it)`` sets the BC vectors to
+    ``base + scale[it] * vec`` (packed u_left | u_right | u_top | u_bot |
+    rho_right), given as ``schedule = (base, vec, scale)``.
+
+    initialize: call ``app.initialize(lat)`` first and run iterations
+    0 .. n_iter-1; False: continue from the lattice's current state, with
+    ``scale[k]`` the scale of the k-th iteration run.  Returns the raw
+    drag/lift sums (fx, fy) of every obstacle in ``app.obstacles`` after
+    every iteration's set_bc, shape (n_iter, n_obs, 2): ``lattice.drag_lift``
+    is ``-2 (fx, fy) / (R L U^2)`` of these.
+    """
+    if initialize:
+        app.initialize(lat)
+    obstacles = list(getattr(app, "obstacles", ()))
+    rec = _Program(obstacles)
+    app.set_bc(rec)
+    prog = np.ascontiguousarray(np.array(rec.ops, dtype=np.int32).reshape(-1, 2))
+    starts = np.zeros(len(obstacles) + 1, dtype=np.int64)
+    links, ps = [], []
+    for k, o in enumerate(obstacles):
+        b = np.asarray(o.boundary, dtype=np.int64).reshape(-1, 3)
+        links.append(b)
+        starts[k + 1] = starts[k] + len(b)
+        ps.append(np.asarray(o.ibb, dtype=np.float64).reshape(-1)[:len(b)] if lat.IBB
+                  else np.zeros(len(b)))
+    links = np.ascontiguousarray(np.concatenate(links) if links else np.zeros((1, 3), np.int64))
+    ps = np.ascontiguousarray(np.concatenate(ps) if ps else np.zeros(1))
+    if lat.IBB and len(ps) < starts[-1]:
+        raise ValueError("ibb distances missing")
+    base, vec, scale = schedule
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    vec = None if vec is None else np.ascontiguousarray(vec, dtype=np.float64)
+    scale = np.ascontiguousarray(np.asarray(scale, dtype=np.float64)[:n_iter])
+    nx, ny = lat.nx, lat.ny
+    if base.shape != (5 * ny + 4 * nx,) or (vec is not None and vec.shape != base.shape) \
+            or scale.shape != (n_iter,):
+        raise ValueError("schedule shapes")
+    drag = np.zeros((n_iter, max(len(obstacles), 1), 2))
+    names = ["g", "g_eq", "g_up", "rho", "u", "u_left", "u_right", "u_top", "u_bot", "rho_right"]
+    arrs = [lat._c(k) for k in names]
+    rc = lib().oracle_run(*[_dp(a) for a in arrs], nx, ny, lat.om_p_lbm, lat.om_m_lbm,
+                          int(bool(lat.IBB)),
+                          prog.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(prog),
+                          _lp(links), _lp(starts), _dp(ps), len(obstacles), _dp(base),
+                          _dp(vec) if vec is not None else None, _dp(scale), n_iter, _dp(drag))
+    if rc != 0:
+        raise IndexError("oracle_run: link or program entry out of range")
+    return drag[:, :len(obstacles)]
 
 
 def run(lattice, app, n_iter=None):

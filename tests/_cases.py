@@ -100,3 +100,39 @@ def max_rel(a, b):
     if np.any(d[zero] > 0):
         return np.inf
     return float(np.max(d[~zero] / den[~zero])) if np.any(~zero) else 0.0
+
+
+def perturb_initial_state(app, eps, seed):
+    """Wrap app.initialize so that g(0) = g_eq(0) * (1 + eps * U(-1, 1)),
+    seeded: the same start for the oracle and the GPU lattice, with
+    non-equilibrium populations in every cell from the first iteration."""
+    orig = app.initialize
+
+    def init(lat):
+        orig(lat)
+        if eps:
+            rng = np.random.default_rng(seed)
+            g = lat.g
+            lat.g = g * (1.0 + eps * (2.0 * rng.random(g.shape) - 1.0))
+
+    app.initialize = init
+    return app
+
+
+def run_oracle_program(app, n):
+    """Iterations 0 .. n-1 of the app on the oracle in one C call
+    (oracle.run_program), links from the vectorised builder (pinned to the
+    cell loops by test_geometry).  Returns the oracle lattice and the raw
+    per-obstacle drag/lift sums, shape (n, n_obstacles, 2)."""
+    from lbm_gb300 import geometry
+    from oracle import oracle as O
+
+    class _Lat(O.OracleLattice):
+        def add_obstacle(self, obstacle):
+            return geometry.add_obstacle(self, obstacle.polygon, obstacle.tag, self.IBB)
+
+    with tempfile.TemporaryDirectory() as td, contextlib.redirect_stdout(io.StringIO()):
+        lat = _Lat(app, output_dir=os.path.join(td, ""))
+        base, vec, scale = app.bc_schedule(lat)
+        drag = O.run_program(lat, app, n, (base, vec, scale(np.arange(n))))
+    return lat, drag

@@ -65,3 +65,21 @@ def test_vectorised_matches_cell_loops(seed):
         assert np.array_equal(ra[2], rb[2])
         assert ra[0] == rb[0]
         assert np.array_equal(lat_a.lattice, lat_b.lattice)
+
+
+@pytest.mark.parametrize("k", [0, 137, 399])
+def test_obstacle_array_squares_match_cell_loops(k):
+    """Squares of the obstacle-array workload (ny 128: 2-cell squares; the
+    parity tests use the vectorised links at ny 256 and 2048)."""
+    from lbm_gb300.apps import obstacle_array
+    app = obstacle_array(L_lbm=128)
+    obs = app.obstacles[k]
+    s = geometry.generate_shape(obs.n_pts, obs.pos, obs.type, obs.size, obs.name, obs.n_spts)
+    lat_a, lat_b = _lat(app), _lat(app)
+    ra = geometry.add_obstacle(lat_a, s.curve_pts, k + 1, True)
+    rb = O.add_obstacle_loops(lat_b, s.curve_pts, k + 1, True)
+    assert len(rb[1]) > 0
+    assert np.array_equal(ra[1], rb[1])
+    assert np.array_equal(ra[2], rb[2])
+    assert ra[0] == rb[0]
+    assert np.array_equal(lat_a.lattice, lat_b.lattice)

@@ -63,23 +63,6 @@ def test_fused_chunking_and_graphs_are_bit_identical(cuda, case, precision):
         assert np.array_equal(h, h_ref)
 
 
-@pytest.mark.parametrize("precision", PLAIN)
-def test_config0_cavity200_vs_oracle(cuda, precision):
-    """Cavity 200x200, u_lid = 0.1, Re = 100, 1000 iterations: <= 1e-12 on f."""
-    from lbm_gb300.apps import cavity
-    def mk():
-        a = cavity()
-        a.L_lbm, a.u_lbm, a.Re_lbm = 200, 0.1, 100.0
-        a.compute_lbm_parameters()
-        a.stop, a.it_max, a.output_freq = "it", 999, 10 ** 12
-        return a
-    lat, _ = run_oracle(mk())
-    out, _, _ = run_gpu(mk(), fused=True, precision=precision)
-    assert max_rel(out["g"], lat.g) <= TOL
-    assert max_rel(out["g_up"], lat.g_up) <= TOL
-    assert max_rel(out["rho"], lat.rho) <= TOL
-
-
 def _tiny_cavity(n):
     from lbm_gb300.apps import cavity
     a = cavity()
