@@ -23,7 +23,9 @@ workload (``f64``: FP64 storage and arithmetic, bounded by the FP64 pipe,
 reported with that second bound); ``form_errors`` runs the cylinder channel
 (ny 200, nx 1100, Re 100) in every form and states the error of each against
 the FP64 run; ``array_form_errors`` (``--array-errors N``, off by default)
-does the same on this workload for N iterations; ``plain_vs_oracle`` checks
+does the same on this workload for N iterations; ``app_api`` runs the
+channel through ``lbm_gb300.run`` with the app's hooks (observables, moving
+averages, drag_lift lines) beside the engine-only figure; ``plain_vs_oracle`` checks
 the plain forms' Cd/Cl series over the whole channel run against the C
 oracle (run in a child process on the host cores meanwhile: the oracle is
 the checker there, never the thing measured); ``batched_sweep`` is the
@@ -90,6 +92,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--sweep-steps", type=int, default=10000,
                     help="iterations of the 256-case batched sweep (0 = skip)")
+    ap.add_argument("--app-steps", type=int, default=200000,
+                    help="iterations of the app-API run of the cylinder channel (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain-oracle", action="store_true",
                     help="skip the oracle run of the channel behind plain_vs_oracle")
@@ -461,6 +465,32 @@ def measure_form_errors(steps, forms, tmp, ny=200):
     return out, plain
 
 
+def measure_app_api(steps, tmp, engine_mlups, ny=200):
+    """The cylinder channel (config 1) through the app API: lbm_gb300.run
+    with the turek app's hooks (drag/lift every iteration, the buffers'
+    moving averages and convergence test, one drag_lift line per iteration),
+    wall time from run() to its return, against the engine-only figure of
+    the same case (run_case).  Field outputs are off (output_freq beyond the
+    run): they are the app's file writes, not the lattice update."""
+    import lbm_gb300
+    app = channel_app(ny, steps)
+    out = tempfile.mkdtemp(prefix="app_api_", dir=tmp)
+    with contextlib.redirect_stdout(io.StringIO()):
+        lat = lbm_gb300.lattice(app, precision="q60", output_dir=out + "/", verbose=False)
+        lat.generate_image = lambda obstacles: None
+        t0 = time.perf_counter()
+        lbm_gb300.run(lat, app)
+        wall = time.perf_counter() - t0
+    with open(os.path.join(out, "drag_lift")) as f:
+        n_lines = sum(1 for _ in f)
+    mlups = lat.nx * lat.ny * steps / wall / 1e6
+    return {"case": "lbm_gb300.run(lattice, turek) on the cylinder channel %dx%d, %d iterations, "
+                    "q60" % (lat.nx, lat.ny, steps),
+            "wall_s": wall, "mlups": mlups, "engine_mlups": engine_mlups,
+            "frac_of_engine": mlups / engine_mlups if engine_mlups else None,
+            "drag_lift_lines": n_lines}
+
+
 def measure_adjoint(steps, tmp, ny=100):
     """Gradient of the mean Cd over the last half of `steps` iterations with
     respect to the inlet profile (every inlet row) and the TRT rate, on the
@@ -747,6 +777,16 @@ def main():
         form_errors, plain_series = measure_form_errors(args.error_steps, FORMS, tmp)
         torch.cuda.empty_cache()
 
+    app_api = None
+    if rank == 0 and args.app_steps > 0:
+        if form_errors and "q60" in form_errors and args.app_steps == args.error_steps:
+            eng_mlups = form_errors["q60"]["mlups"]
+        else:
+            eng_mlups = run_case(channel_app(200, args.app_steps), "q60", args.app_steps,
+                                 tmp)["mlups"]
+        app_api = measure_app_api(args.app_steps, tmp, eng_mlups)
+        torch.cuda.empty_cache()
+
     array_errors = None
     if rank == 0 and args.array_errors > 0:
         array_errors = measure_array_errors(args.array_errors, FORMS, tmp, args.ny)
@@ -792,7 +832,7 @@ def main():
         "kernel_ms": res["kernel_ms"], "e2e": e2e,
         "gpu_launches": args.steps * res["kernels_per_step"],
         "clocks": clocks, "forms": forms, "form_errors": form_errors,
-        "plain_vs_oracle": plain_oracle,
+        "plain_vs_oracle": plain_oracle, "app_api": app_api,
         "array_form_errors": array_errors,
         "batched_sweep": sweep, "adjoint": adjoint, "cpu_baseline": cpu,
     }

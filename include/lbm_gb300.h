@@ -111,6 +111,18 @@ int lbm_drag_lift_f64(const int32_t* links, int64_t n, const double* g_up, const
 #define LBM_DRAG_NOALLOC_MAX_LINKS 1048576
 int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const double* g_up,
                               const double* g, int nx, int ny, double* out, void* stream);
+/* buff.mv_avg (lbm/src/utils/buff.py:35-77) after each of n adds, on the
+ * device.  hist: [4][cap] doubles, the histories buff, avg1, avg2, avg3 of
+ * the reference (each starting with two zeros; add m is stored at index
+ * m + 1).  The caller has stored adds k0 + 1 .. k0 + n in hist[0] and has
+ * made k0 adds before (k0 + n + 2 <= cap).  For each add t: obs[t] (the
+ * returned average), growth[t] and cv[t] (the obs_cv flag after it); the
+ * averages are appended to avg1..avg3.  state: [2] ints, the convergence
+ * counter and flag, carried between calls (zero at the start).  Sums are in
+ * NumPy's pairwise order, so every value equals the reference's bit for bit. */
+int lbm_mv_avg_chunk(double* hist, int64_t cap, int64_t k0, int32_t n, double dt, double cv_ct,
+                     int32_t cv_nb, int32_t* state, double* obs, double* growth, int32_t* cv,
+                     void* stream);
 /* Zou-He walls, lbm/src/core/nb.py:121-247.  wall: LBM_WALL_*; vec is the
  * wall's (2 x len) velocity vector; rho_right only for RIGHT_PRESSURE. */
 int lbm_zou_he_f64(int wall, double* u, double* rho, double* g, const double* vec,

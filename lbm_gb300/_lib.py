@@ -104,6 +104,8 @@ _SIGS = {
                                   ctypes.c_int),
     "lbm_zou_he_f64": ([ctypes.c_int, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp],
                        ctypes.c_int),
+    "lbm_mv_avg_chunk": ([_vp, _i64, _i64, _i32, _d, _d, _i32, _vp, _vp, _vp, _vp, _vp],
+                         ctypes.c_int),
     "lbm_zou_he_corner_f64": ([ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp],
                               ctypes.c_int),
     "lbm_problem_scratch_bytes": ([ctypes.POINTER(Problem)], ctypes.c_size_t),

@@ -125,6 +125,80 @@ class turek(_channel):
         drag, lift = lattice.drag_lift(self.obstacles[0], self.rho_lbm, self.u_avg, self.D_lbm)
         self.add_buff(drag, lift, lattice, it)
 
+    def observables_chunk(self, lattice, first, rows, obstacles, stop_check=True):
+        """``observables`` (and ``check_stop`` when stop_check) of iterations
+        first .. first + len(rows) - 1 at once, for the fused runner.
+
+        rows[k, o] is the raw (fx, fy) of obstacles[o] (the runner's list, in
+        set_bc order) at iteration first + k: what ``lattice.drag_lift``
+        normalises.  The coefficients, the buffers' moving averages (on the
+        GPU, ``buff.add_chunk``) and the drag_lift lines are those of the
+        per-iteration calls, bit for bit.  Returns the iteration at which
+        check_stop ends the run (the observables stop there too) or None.
+        """
+        n = len(rows)
+        if n == 0:
+            return None
+        o = next(k for k, ob in enumerate(obstacles) if ob is self.obstacles[0])
+        den = self.rho_lbm * self.D_lbm * self.u_avg ** 2
+        cx = -2.0 * rows[:, o, 0] / den
+        cy = -2.0 * rows[:, o, 1] / den
+        saved = [(b.it, b.obs, b.obs_cv_cnt, b.obs_cv,
+                  None if b._state is None else b._state.clone())
+                 for b in (self.drag_buff, self.lift_buff)]
+        ax, gx, vx = self.drag_buff.add_chunk(cx)
+        ay, gy, vy = self.lift_buff.add_chunk(cy)
+        its = np.arange(first, first + n)
+        stop = None
+        if stop_check:
+            if self.stop == "obs":
+                hit = np.flatnonzero(vx & vy)
+            elif self.stop == "it":
+                hit = np.flatnonzero(its >= self.it_max)
+            else:
+                hit = np.zeros(0, np.int64)
+            if len(hit):
+                t = int(hit[0])
+                stop = first + t
+                if t < n - 1:
+                    # the run ends inside the chunk: redo the buffers up to it
+                    for b, (it0, obs, cnt, cv, st) in zip((self.drag_buff, self.lift_buff),
+                                                          saved):
+                        b.it, b.obs, b.obs_cv_cnt, b.obs_cv = it0, obs, cnt, cv
+                        if st is not None:
+                            b._state.copy_(st)
+                        else:
+                            b._state = None
+                    ax, gx, _ = self.drag_buff.add_chunk(cx[:t + 1])
+                    ay, gy, _ = self.lift_buff.add_chunk(cy[:t + 1])
+                    its, cx, cy = its[:t + 1], cx[:t + 1], cy[:t + 1]
+                self.check_stop(stop)
+        self._write_lines(its * self.dt, cx, cy, ax, ay, gx, gy)
+        return stop
+
+    def _write_lines(self, *cols):
+        """Append drag_lift lines ('{} {} {} {} {} {} {}' of the columns) from
+        a writer thread, in submission order, after any pending lines."""
+        import concurrent.futures
+        if getattr(self, "_writer", None) is None:
+            self._writer = concurrent.futures.ThreadPoolExecutor(1)
+            self._writes = []
+        cols = [np.asarray(c, dtype=np.float64).copy() for c in cols]
+        path = self._dl_file
+        pending = self._lines
+        self._lines = []
+
+        def work():
+            strs = [list(map(repr, c.tolist())) for c in cols]
+            text = "".join(pending) + "".join(" ".join(t) + "\n" for t in zip(*strs))
+            with open(path, "a") as f:
+                f.write(text)
+
+        for w in [w for w in self._writes if w.done()]:
+            w.result()  # raises a failed write here
+        self._writes = [w for w in self._writes if not w.done()]
+        self._writes.append(self._writer.submit(work))
+
     def add_buff(self, Cx, Cy, lattice, it):
         self.drag_buff.add(Cx)
         self.lift_buff.add(Cy)
@@ -136,6 +210,9 @@ class turek(_channel):
             self.flush_observables()
 
     def flush_observables(self):
+        for w in getattr(self, "_writes", ()):
+            w.result()
+        self._writes = []
         if getattr(self, "_lines", None):
             with open(self._dl_file, "a") as f:
                 f.writelines(self._lines)

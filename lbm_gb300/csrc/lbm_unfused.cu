@@ -434,6 +434,155 @@ extern "C" int lbm_drag_lift_f64_noalloc(const int32_t* links, int64_t n, const 
   return LBM_OK;
 }
 
+// ---- observable buffer: buff.mv_avg for a chunk of adds ----------------------
+// lbm/src/utils/buff.py:35-77.  After add number k (k = 1, 2, ...) the
+// reference computes, with it_s = floor(4k/5) and windows [it_s, k) of its
+// histories (each starts with two zeros, so add m is stored at index m + 1):
+//   obs1 = sum(buff[it_s:k]) / (k - it_s + 1)    appended to avg1
+//   obs2 = sum(avg1[it_s:k]) / (k - it_s + 1)    appended to avg2
+//   obs3 = sum(avg2[it_s:k]) / (k - it_s + 1)    appended to avg3
+//   obs  = sum(avg3[it_s:k]) / (k - it_s + 1)    returned
+// and, for k > 10, growth = (avg3[k] - avg3[it_s]) / ((k - it_s + 1) dt) with
+// the convergence counter.  A level's window for add k reads the level below
+// up to index k - 1, i.e. values of adds <= k - 2, so each level of a chunk
+// of adds is computed in parallel (one thread per add) once the level below
+// is complete.  Sums follow NumPy's order for a contiguous float64 slice
+// (pairwise summation: blocks of at most 128 values summed with eight
+// accumulators, longer ranges split in two with the first length a multiple
+// of 8), so every value equals the reference's bit for bit.
+namespace lbm {
+namespace mvavg {
+
+__device__ double pw_block(const double* a, long long n) {
+  if (n < 8) {
+    double r = 0.0;
+    for (long long i = 0; i < n; ++i) r += a[i];
+    return r;
+  }
+  double r0 = a[0], r1 = a[1], r2 = a[2], r3 = a[3], r4 = a[4], r5 = a[5], r6 = a[6], r7 = a[7];
+  long long i = 8;
+  for (; i < n - (n % 8); i += 8) {
+    r0 += a[i];
+    r1 += a[i + 1];
+    r2 += a[i + 2];
+    r3 += a[i + 3];
+    r4 += a[i + 4];
+    r5 += a[i + 5];
+    r6 += a[i + 6];
+    r7 += a[i + 7];
+  }
+  double res = ((r0 + r1) + (r2 + r3)) + ((r4 + r5) + (r6 + r7));
+  for (; i < n; ++i) res += a[i];
+  return res;
+}
+
+__device__ __forceinline__ long long pw_split(long long n) {
+  long long n2 = n / 2;
+  return n2 - n2 % 8;
+}
+
+// Pairwise sum of a[0..n) without recursion: a stack of the ranges whose
+// left half is being summed (at most 57 levels for any 64-bit length).
+__device__ double pw_sum(const double* a, long long n) {
+  if (n <= 128) return pw_block(a, n);
+  const double* sa[64];
+  long long sn[64];
+  double sl[64];
+  bool sdone[64];
+  int top = 0;
+  sa[0] = a;
+  sn[0] = n;
+  sdone[0] = false;
+  for (;;) {
+    // descend into left halves down to a block
+    while (sn[top] > 128) {
+      const long long n2 = pw_split(sn[top]);
+      sa[top + 1] = sa[top];
+      sn[top + 1] = n2;
+      sdone[top + 1] = false;
+      ++top;
+    }
+    double v = pw_block(sa[top], sn[top]);
+    --top;
+    // go up: a finished left half starts its right sibling, a finished
+    // right half completes its parent
+    for (;;) {
+      if (top < 0) return v;
+      if (!sdone[top]) {
+        const long long n2 = pw_split(sn[top]);
+        sl[top] = v;
+        sdone[top] = true;
+        sa[top + 1] = sa[top] + n2;
+        sn[top + 1] = sn[top] - n2;
+        sdone[top + 1] = false;
+        ++top;
+        break;
+      }
+      v = sl[top] + v;
+      --top;
+    }
+  }
+}
+
+// Level `level` (1..4) of adds k0 + 1 .. k0 + n.  hist: [4][cap] (buff, avg1,
+// avg2, avg3).  Levels 1-3 append to the next history; level 4 writes obs.
+__global__ void k_mv_avg_level(double* hist, long long cap, long long k0, int n, int level,
+                               double* obs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long k = k0 + 1 + t;
+  const long long it_s = (4 * k) / 5;
+  const double v = pw_sum(hist + (long long)(level - 1) * cap + it_s, k - it_s) /
+                   (double)(k - it_s + 1);
+  if (level < 4) hist[(long long)level * cap + k + 1] = v;
+  else obs[t] = v;
+}
+
+// Growth rates and the convergence counter, in order (one thread).
+// state: [0] counter, [1] converged flag (kept across calls).
+__global__ void k_mv_avg_growth(const double* hist, long long cap, long long k0, int n, double dt,
+                                double cv_ct, int cv_nb, int* state, double* growth, int* cv) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const double* avg3 = hist + 3 * cap;
+  int cnt = state[0], flag = state[1];
+  for (int t = 0; t < n; ++t) {
+    const long long k = k0 + 1 + t;
+    double g = 0.0;
+    if (k > 10) {
+      const long long it_s = (4 * k) / 5;
+      const double db = avg3[k] - avg3[it_s];
+      g = db / ((double)(k - it_s + 1) * dt);
+      cnt = fabs(g) < cv_ct ? cnt + 1 : 0;
+      if (cnt > cv_nb) flag = 1;
+    }
+    growth[t] = g;
+    cv[t] = flag;
+  }
+  state[0] = cnt;
+  state[1] = flag;
+}
+
+}  // namespace mvavg
+}  // namespace lbm
+
+extern "C" int lbm_mv_avg_chunk(double* hist, int64_t cap, int64_t k0, int32_t n, double dt,
+                                double cv_ct, int32_t cv_nb, int32_t* state, double* obs,
+                                double* growth, int32_t* cv, void* stream) {
+  if (!hist || !state || !obs || !growth || !cv || n < 0 || k0 < 0 || k0 + n + 2 > cap) {
+    set_error("lbm_mv_avg_chunk: bad arguments (k0 %lld, n %d, capacity %lld)", (long long)k0,
+              (int)n, (long long)cap);
+    return LBM_ERR_ARG;
+  }
+  if (n == 0) return LBM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int tb = 128;
+  for (int level = 1; level <= 4; ++level)
+    lbm::mvavg::k_mv_avg_level<<<(n + tb - 1) / tb, tb, 0, st>>>(hist, cap, k0, n, level, obs);
+  lbm::mvavg::k_mv_avg_growth<<<1, 1, 0, st>>>(hist, cap, k0, n, dt, cv_ct, cv_nb, state, growth, cv);
+  LBM_LAUNCH_CHECK("lbm_mv_avg_chunk");
+  return LBM_OK;
+}
+
 extern "C" int lbm_zou_he_f64(int wall, double* u, double* rho, double* g, const double* vec,
                               const double* rho_right, int nx, int ny, void* stream) {
   if (int rc = check_grid("lbm_zou_he_f64", nx, ny)) return rc;

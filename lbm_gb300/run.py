@@ -14,7 +14,9 @@ hooks are replayed in order after each chunk:
 * ``outputs``     chunks end at multiples of ``app.output_freq``, where the
   step writes macro rho/u, so the hook sees the reference fields;
 * ``observables`` ``lattice.drag_lift`` returns the drag/lift the device
-  computed for that iteration;
+  computed for that iteration; apps with ``observables_chunk`` (turek) take
+  a whole chunk at once (moving averages on the device, lines written by a
+  writer thread) instead of one Python call per iteration;
 * ``check_stop``  when it stops inside a chunk, the chunk is re-run from a
   snapshot up to the stop iteration.
 
@@ -111,11 +113,31 @@ def run_fused(lattice, app, chunk=1000, graph=True, n_iter=None, verbose=True):
             eng.steps(first, last_it - first + 1, macro_last=macro_last, graph=use_graph)
 
     replay = _Replay(obstacles)
+    # Apps that take a chunk of observables at once (observables_chunk) skip
+    # the per-iteration replay: their outputs act only at multiples of
+    # output_freq, and the hook evaluates check_stop itself.
+    chunk_obs = getattr(app, "observables_chunk", None)
+
+    def replay_chunk(first, last_avail, honour_stop):
+        rows = eng.drag_rows(first, last_avail)
+        if out_freq:
+            m = max(first, state["outputs_done"] + 1)
+            m = -(-m // out_freq) * out_freq
+            while m <= last_avail:
+                app.outputs(lattice, m)
+                state["outputs_done"] = m
+                m += out_freq
+        stop = chunk_obs(lattice, first, rows, obstacles, stop_check=honour_stop)
+        if honour_stop and stop is None and n_iter is not None and first <= n_iter - 1 <= last_avail:
+            stop = n_iter - 1
+        return stop
 
     def replay_hooks(first, last_avail, honour_stop=True):
         """outputs/observables/check_stop of first..last_avail; stop iteration or None."""
         if last_avail < first:
             return None
+        if chunk_obs is not None:
+            return replay_chunk(first, last_avail, honour_stop)
         rows = eng.drag_rows(first, last_avail)
         lattice._replay = replay
         try:
@@ -154,6 +176,7 @@ def run_fused(lattice, app, chunk=1000, graph=True, n_iter=None, verbose=True):
         snap = eng.snapshot() if known_stop is None else None
         first = last + 1
         steps(first, e, macro_last=is_output(e) or e == known_stop, use_graph=graph)
+        torch.cuda.synchronize()  # waits without the GIL (the apps' writer threads run)
         eng.check_status()
         stop = replay_hooks(pending, e - 1)
         if stop is not None:
@@ -181,6 +204,8 @@ def run_fused(lattice, app, chunk=1000, graph=True, n_iter=None, verbose=True):
         ensure_scale(last + 1)
     _finalize_state(lattice, eng, last)
     replay_hooks(pending, last, honour_stop=False)
+    if chunk_obs is not None and known_stop is not None and last == known_stop:
+        app.check_stop(last)  # the per-iteration replay's last call (its message)
     if sched is not None:
         app.set_inlets(lattice, last)
     lattice._engine = eng
