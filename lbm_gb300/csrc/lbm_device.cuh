@@ -469,6 +469,67 @@ __device__ __forceinline__ void collide(T d[9], const Moments<T, SHIFT>& m, cons
 }
 
 // ---------------------------------------------------------------------------
+// Two cells at once in packed FP32 (the FADD2 / FMUL2 / FFMA2 instructions of
+// sm_100 and later: one instruction for both elements of a float2).  Each
+// element goes through the operations of moments() and collide() on float;
+// the bulk kernels of the reduced forms, which update cells in pairs anyway
+// (packed conversions on store), use these to halve their FP32 instruction
+// count.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b: b * -1 is exact, so the fused multiply-add rounds a - b once.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+struct Moments2 {
+  float2 drho, rho, jx, jy, ux, uy;
+};
+
+// moments<float, SHIFT>() of two cells (d[q].x: first cell, .y: second).
+template <bool SHIFT>
+__device__ __forceinline__ Moments2 moments2(const float2 d[9], float rho0, float inv_scale) {
+  Moments2 m;
+  const float2 s12 = add2(d[1], d[2]), s34 = add2(d[3], d[4]), s56 = add2(d[5], d[6]),
+               s78 = add2(d[7], d[8]);
+  const float2 d12 = sub2(d[1], d[2]), d34 = sub2(d[3], d[4]), d56 = sub2(d[5], d[6]),
+               d87 = sub2(d[8], d[7]);
+  m.drho = add2(add2(add2(add2(d[0], s12), s34), s56), s78);
+  m.rho = SHIFT ? fma2(m.drho, f2(inv_scale), f2(rho0)) : m.drho;
+  m.jx = add2(add2(d12, d56), d87);
+  m.jy = sub2(add2(d34, d56), d87);
+  const float2 r = mul2(make_float2(recip(m.rho.x), recip(m.rho.y)), f2(inv_scale));
+  m.ux = mul2(m.jx, r);
+  m.uy = mul2(m.jy, r);
+  return m;
+}
+
+// collide<float, SHIFT>() of two cells.
+__device__ __forceinline__ void collide2(float2 d[9], const Moments2& m, const Coef<float>& k) {
+  const float2 jx = m.jx, jy = m.jy, ux = m.ux, uy = m.uy;
+  const float2 Qx = mul2(jx, ux), Qy = mul2(jy, uy);
+  const float2 j5 = add2(jx, jy), u5 = add2(ux, uy), Q5 = mul2(j5, u5);
+  const float2 j7 = sub2(jy, jx), u7 = sub2(uy, ux), Q7 = mul2(j7, u7);
+  const float2 R = fma2(f2(-1.5f), add2(Qx, Qy), m.drho);
+  d[0] = fma2(f2(k.a0), d[0], mul2(f2(k.p0), R));
+#define LBM_PAIR2(q, qb, Q, cj, wp, wm)                                  \
+  {                                                                      \
+    const float2 P = fma2(f2(4.5f), Q, R);                               \
+    const float2 M = mul2(f2(wm), cj);                                   \
+    const float2 base = mul2(f2(wp), P);                                 \
+    const float2 dq = d[q], dqb = d[qb];                                 \
+    d[q] = fma2(f2(k.a), dq, fma2(f2(k.mb), dqb, add2(base, M)));        \
+    d[qb] = fma2(f2(k.a), dqb, fma2(f2(k.mb), dq, sub2(base, M)));       \
+  }
+  LBM_PAIR2(1, 2, Qx, jx, k.wp1, k.wm1)
+  LBM_PAIR2(3, 4, Qy, jy, k.wp1, k.wm1)
+  LBM_PAIR2(5, 6, Q5, j5, k.wp2, k.wm2)
+  LBM_PAIR2(7, 8, Q7, j7, k.wp2, k.wm2)
+#undef LBM_PAIR2
+}
+
+// ---------------------------------------------------------------------------
 // Boundary operations on full (unshifted) populations of one cell, written in
 // the operation order of the reference expressions.
 // ---------------------------------------------------------------------------

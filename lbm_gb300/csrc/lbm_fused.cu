@@ -31,8 +31,12 @@ __global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
   if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
+// Resident 128-thread blocks per SM the vectorised bulk kernel is compiled for.
+#ifndef LBM_VEC_MIN_BLOCKS
+#define LBM_VEC_MIN_BLOCKS 1
+#endif
 template <class St, int V>
-__global__ void __launch_bounds__(128) k_bulk_vec(FusedArgs a) {
+__global__ void __launch_bounds__(128, LBM_VEC_MIN_BLOCKS) k_bulk_vec(FusedArgs a) {
   const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   bulk_group_vec<St, V>(a, gi);
   if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);

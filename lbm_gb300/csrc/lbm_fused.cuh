@@ -2,6 +2,8 @@
 // single-lattice kernels (lbm_fused.cu) and the batched persistent kernels
 // (lbm_batch.cu).  See lbm_fused.cu for the scheme.
 #pragma once
+#include <type_traits>
+
 #include "lbm_device.cuh"
 #include "lbm_internal.h"
 
@@ -226,6 +228,13 @@ __device__ __forceinline__ void bulk_cell(const FusedArgs& a, long long cell) {
 // with placeholder values and then overwritten by k_special, as in k_bulk,
 // and padding cells (j >= ny) hold values no real cell ever reads.
 // ---------------------------------------------------------------------------
+// 1: the vectorised bulk kernels of the FP32-arithmetic forms update a pair
+// of cells with packed FP32 instructions (moments2 / collide2); 0: one cell
+// at a time.
+#ifndef LBM_VEC_PAIRED
+#define LBM_VEC_PAIRED 1
+#endif
+
 template <typename S, int V>
 struct alignas(sizeof(S) * V) Pack {
   S v[V];
@@ -282,6 +291,62 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
   // random stream of a pair starts from its first cell's storage index, so
   // the bits do not depend on V.
   const unsigned it_hash = St::kStochastic ? sr_iter(*a.it_dev) : 0u;
+  if constexpr (LBM_VEC_PAIRED && std::is_same<T, float>::value) {
+    // Both cells of a pair in packed FP32 (moments2 / collide2).
+#pragma unroll
+    for (int e = 0; e < V; e += 2) {
+      unsigned r = St::kStochastic ? sr_cell((long long)i * sy + j0 + e, it_hash) : 0u;
+      float2 d2[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        T v[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int c = e + h;
+          if (cy(q) == 1) {
+            v[h] = c == 0 ? halo[q] : St::load(&in[q].v[c - 1]);
+          } else if (cy(q) == -1) {
+            v[h] = c == V - 1 ? halo[q] : St::load(&in[q].v[c + 1]);
+          } else {
+            v[h] = St::load(&in[q].v[c]);
+          }
+        }
+        d2[q] = make_float2(v[0], v[1]);
+      }
+      const Moments2 m = moments2<St::kShift>(d2, k.rho0, St::kInvScale);
+      const int ja = j0 + e, jb = ja + 1;
+      if (a.write_macro) {
+        if (ja < ny) {
+          const long long rc = (long long)i * ny + ja;
+          a.rho_out[rc] = (double)m.rho.x;
+          a.u_out[rc] = (double)m.ux.x;
+          a.u_out[N + rc] = (double)m.uy.x;
+        }
+        if (jb < ny) {
+          const long long rc = (long long)i * ny + jb;
+          a.rho_out[rc] = (double)m.rho.y;
+          a.u_out[rc] = (double)m.ux.y;
+          a.u_out[N + rc] = (double)m.uy.y;
+        }
+      }
+      // Wall cells are checked by k_special, which recomputes them.
+      if (a.check_finite) {
+        const float2 chk = add2(add2(m.rho, m.ux), m.uy);
+        if ((ja > 0 && ja < ny - 1 && !isfinite(chk.x)) ||
+            (jb > 0 && jb < ny - 1 && !isfinite(chk.y)))
+          atomicOr(a.status, 1u);
+      }
+      collide2(d2, m, k);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        // padding (j >= ny): keep the stored deviations at zero
+        if (ja >= ny) d2[q].x = 0.0f;
+        if (jb >= ny) d2[q].y = 0.0f;
+        if (St::kStochastic) r = lcg32(r);
+        St::store_pair(&out[q].v[e], d2[q].x, d2[q].y, r);
+      }
+    }
+  } else {
 #pragma unroll
   for (int e = 0; e < V; e += 2) {
     unsigned r = St::kStochastic ? sr_cell((long long)i * sy + j0 + e, it_hash) : 0u;
@@ -323,6 +388,7 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
       if (St::kStochastic) r = lcg32(r);
       St::store_pair(&out[q].v[e], dd[0][q], dd[1][q], r);
     }
+  }
   }
   S* fout = (S*)a.fout;
 #pragma unroll
