@@ -429,11 +429,61 @@ def measure_array_errors(steps, forms, tmp, ny):
     return out
 
 
+def shedding_period(cl):
+    """Mean distance in iterations between upward zero crossings of the
+    lift about its mean (None without at least three)."""
+    s = np.sign(cl - cl.mean())
+    up = np.flatnonzero((s[:-1] < 0) & (s[1:] >= 0))
+    return float(np.mean(np.diff(up))) if len(up) >= 3 else None
+
+
+def aligned_lag(ref, got, max_lag):
+    """The shift L (|L| <= max_lag) that best aligns got[t + L] with ref[t]
+    (largest mean product of the mean-free series over their overlap; the
+    correlations by FFT)."""
+    a = ref - ref.mean()
+    b = got - got.mean()
+    n = len(a)
+    m = 1 << int(np.ceil(np.log2(2 * n)))
+    c = np.fft.irfft(np.fft.rfft(b, m) * np.conj(np.fft.rfft(a, m)), m)
+    lags = np.arange(-max_lag, max_lag + 1)
+    # mean product over the overlap of each shift
+    return int(lags[np.argmax(c[lags % m] / (n - np.abs(lags)))])
+
+
+def series_errors(ref_cd, ref_cl, cd, cl, period):
+    """Max deviation of the Cd / Cl series relative to the series' maximum
+    magnitude, as they are and after shifting the form's series by the lag
+    that aligns its shedding phase with the reference's."""
+    out = {"cd_series_max_rel": float(np.max(np.abs(cd - ref_cd)) / np.max(np.abs(ref_cd))),
+           "cl_series_max_rel": float(np.max(np.abs(cl - ref_cl)) / np.max(np.abs(ref_cl)))}
+    if period:
+        # the phase is defined up to whole periods: the smallest shift, then
+        # the least-squares shift of Cl near it
+        lag0 = aligned_lag(ref_cl, cl, int(period // 2))
+
+        def sq(L):
+            n = len(ref_cl) - abs(L)
+            a0, b0 = (0, L) if L >= 0 else (-L, 0)
+            return float(np.mean((cl[b0:b0 + n] - ref_cl[a0:a0 + n]) ** 2))
+
+        lag = min(range(lag0 - 32, lag0 + 33), key=sq)
+        n = len(ref_cl) - abs(lag)
+        r0, g0 = (0, lag) if lag >= 0 else (-lag, 0)
+        out["phase_lag_iterations"] = lag
+        for k, rs, gs in (("cd", ref_cd, cd), ("cl", ref_cl, cl)):
+            d = np.abs(gs[g0:g0 + n] - rs[r0:r0 + n])
+            out[k + "_aligned_max_rel"] = float(d.max() / np.max(np.abs(rs[r0:r0 + n])))
+    return out
+
+
 def measure_form_errors(steps, forms, tmp, ny=200):
-    """Every form on the cylinder channel, errors stated against the FP64 run:
-    velocity-field L2 at the last iteration, and mean Cd / rms Cl / max Cd /
-    max Cl over the second half of the run.  Also returns the Cd/Cl series
-    and final velocity of the two plain forms (f64, q60) for plain_vs_oracle."""
+    """Every form on the cylinder channel, errors stated against the FP64 run
+    over the second half of the run: mean Cd, rms Cl, max Cd, max Cl, the
+    Cd oscillation amplitude and the shedding period; the whole Cd and Cl
+    series (max deviation, as they are and phase-aligned); the velocity
+    field at the last iteration (L2).  Also returns the Cd/Cl series and
+    final velocity of the two plain forms (f64, q60) for plain_vs_oracle."""
     import torch
     ref = run_channel("f64", ny, steps, tmp)
     half = slice(len(ref["cd"]) // 2, None)
@@ -441,11 +491,14 @@ def measure_form_errors(steps, forms, tmp, ny=200):
     def stats(r):
         cd, cl = r["cd"][half], r["cl"][half]
         return {"cd_mean": float(cd.mean()), "cl_rms": float(np.sqrt((cl ** 2).mean())),
-                "cd_max": float(cd.max()), "cl_max": float(cl.max())}
+                "cd_max": float(cd.max()), "cl_max": float(cl.max()),
+                "cd_amplitude": float(0.5 * (cd.max() - cd.min())),
+                "period": shedding_period(cl)}
 
     sref = stats(ref)
     out = {"case": "cylinder channel %dx%d, D = %d, Re 100, %d iterations (all forms from the "
-                   "same initial state)" % (ref["nx"], ref["ny"], channel_app(ny, 2).D_lbm, steps),
+                   "same initial state); statistics over the second half" %
+                   (ref["nx"], ref["ny"], channel_app(ny, 2).D_lbm, steps),
            "f64": dict(sref, mlups=ref["mlups"])}
     plain = {"f64": {k: ref[k] for k in ("cd", "cl", "u")}}
     for form in forms:
@@ -455,10 +508,11 @@ def measure_form_errors(steps, forms, tmp, ny=200):
         if form == "q60":
             plain["q60"] = {k: r[k] for k in ("cd", "cl", "u")}
         st = stats(r)
-        err = {k + "_rel": abs(st[k] - sref[k]) / abs(sref[k]) for k in sref}
+        err = {k + "_rel": (abs(st[k] - sref[k]) / abs(sref[k])
+                            if st[k] is not None and sref[k] else None) for k in sref}
         err["u_l2_rel"] = float(np.linalg.norm(r["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
-        err["cd_series_max_rel"] = float(np.max(np.abs(r["cd"] - ref["cd"])) /
-                                         np.max(np.abs(ref["cd"])))
+        err.update(series_errors(ref["cd"][half], ref["cl"][half], r["cd"][half],
+                                 r["cl"][half], sref["period"]))
         out[form] = dict(st, mlups=r["mlups"], error_vs_f64=err)
         del r
         torch.cuda.empty_cache()
