@@ -310,27 +310,33 @@ def measure_e2e(app, lat, eng, it, steps):
 
 
 def measure_sweep(steps):
-    """The 256-case sweep (FP16 shifted storage): autotune, then `steps`
-    iterations of every case in batched graphs; the per-case serial launch
-    loop is timed on 20 iterations for comparison."""
+    """The 256-case sweep (FP16 shifted storage): autotune (scheduling,
+    vector width, threads, tile rounds, then iterations per graph), then
+    `steps` iterations of every case in batched graphs; the per-case serial
+    loop is timed for comparison, with plain launches (20 iterations) and
+    with one CUDA graph per case (50 iterations)."""
     import torch
     from lbm_gb300.batch import Batch, autotune, serial_loop_mlups, sweep_apps, time_batch
     t0 = time.perf_counter()
     # BC schedule length: the timed iterations, the autotuner's trials
     # (20 configurations x 150 iterations) and the serial-loop check.
-    b = Batch(sweep_apps(seed=2024), precision=SWEEP_FORM, max_steps=steps + 6000)
+    b = Batch(sweep_apps(seed=2024), precision=SWEEP_FORM, max_steps=steps + 10000)
     setup_s = time.perf_counter() - t0
-    best, trials = autotune(b, steps=100)
+    best, trials = autotune(b, steps=200)
     b.check()
     ms = time_batch(b, steps, k=best["k_steps"])
     b.check()
     mlups = b.cells * steps / (ms * 1e-3) / 1e6
     serial, _ = serial_loop_mlups(b, steps=20)
+    serial_g, _ = serial_loop_mlups(b, steps=50, graph=True)
     info = b.info()
     b.close()
+    k_trials = {t[0]["k_steps"]: t[1] for t in trials[-5:]}
     return {"cases": info["lattices"], "cells": b.cells, "steps": steps, "mlups": mlups,
             "ms_per_step": ms / steps, "serial_loop_mlups": serial,
-            "x_vs_serial": mlups / serial, "config": best, "setup_s": setup_s,
+            "x_vs_serial": mlups / serial, "serial_graph_loop_mlups": serial_g,
+            "x_vs_serial_graphs": mlups / serial_g, "config": best,
+            "k_steps_trials_mlups": k_trials, "setup_s": setup_s,
             "autotune_trials": len(trials), "precision": SWEEP_FORM,
             "all_finite": True}
 

@@ -211,12 +211,14 @@ def time_batch(batch, n_steps, k=None):
     return e0.elapsed_time(e1)
 
 
-def autotune(batch, steps=60, space=None, verbose=False):
+def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200), verbose=False):
     """Pick the fastest batch configuration by timing candidates.
 
     Every candidate runs ``steps`` iterations after one warm-up launch (which
     also captures its graph); the lattices keep advancing, which does not
-    change the cost per iteration.  Returns (best config, table of trials).
+    change the cost per iteration.  A second stage times the winner with
+    each number of iterations per CUDA graph in ``k_space`` (over the same
+    iteration count for every K).  Returns (best config, table of trials).
     """
     # one block per tile (the persistent grid size does not apply), then
     # persistent blocks; a dict of value lists or a list of such dicts
@@ -248,6 +250,21 @@ def autotune(batch, steps=60, space=None, verbose=False):
             print(cfg, "%.0f MLUPS" % mlups)
         if best is None or mlups > best[1]:
             best = (dict(cfg), mlups)
+    if k_space:
+        n = max(k_space) * max(1, -(-steps // max(k_space)))
+        stage1 = best
+        best = None
+        for k in k_space:
+            cfg = dict(stage1[0], k_steps=k)
+            batch.set_config(cfg)
+            batch.advance(k, k=k)  # warm-up + graph capture
+            ms = time_batch(batch, n, k=k)
+            mlups = batch.cells * n / (ms * 1e-3) / 1e6
+            trials.append((dict(cfg), mlups))
+            if verbose:
+                print(cfg, "%.0f MLUPS" % mlups)
+            if best is None or mlups > best[1]:
+                best = (dict(cfg), mlups)
     batch.set_config(best[0])
     return best[0], trials
 
