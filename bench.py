@@ -319,7 +319,8 @@ def measure_sweep(steps):
     from lbm_gb300.batch import Batch, autotune, serial_loop_mlups, sweep_apps, time_batch
     t0 = time.perf_counter()
     # BC schedule length: the timed iterations, the autotuner's trials
-    # (20 configurations x 150 iterations) and the serial-loop check.
+    # (20 configurations x 250 iterations, then 5 x (K + 200)) and the
+    # serial loops.
     b = Batch(sweep_apps(seed=2024), precision=SWEEP_FORM, max_steps=steps + 10000)
     setup_s = time.perf_counter() - t0
     best, trials = autotune(b, steps=200)
