@@ -54,6 +54,11 @@ struct FusedArgs {
   double* stale[2];         // [9][n_special] post-BC g of an iteration
   double* mac[2];           // [3][n_special] macro rho, ux, uy of an iteration
   double* link_force;       // [2][n_links]
+  // special-first steps of the shifted forms (lbm_problem.special_mask)
+  const unsigned* special_mask;
+  const int* special_rank;
+  void* sbuf;               // [9][n_special] storage elements: special-cell results
+  int special_first;        // this launch runs k_special before the bulk kernel
   int n_links;
   // drag/lift history
   double* drag_hist;
@@ -390,6 +395,27 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
     }
   }
   }
+  if (a.special_first) {
+    // Special cells of this group: their values, computed by k_special into
+    // scratch, go into this group's vectors (the group's V bits lie in one
+    // mask word: groups are V-aligned and V divides 32).
+    const long long c0 = (long long)i * sy + j0;
+    const unsigned word = __ldg(a.special_mask + (c0 >> 5));
+    const unsigned sh = (unsigned)(c0 & 31);
+    const unsigned bits = (word >> sh) & ((1u << V) - 1u);
+    if (bits) {
+      int rank = __ldg(a.special_rank + (c0 >> 5)) + __popc(word & ((1u << sh) - 1u));
+      const S* sb = (const S*)a.sbuf;
+#pragma unroll
+      for (int c = 0; c < V; ++c) {
+        if ((bits >> c) & 1u) {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) out[q].v[c] = sb[(long long)q * a.n_special + rank];
+          ++rank;
+        }
+      }
+    }
+  }
   S* fout = (S*)a.fout;
 #pragma unroll
   for (int q = 0; q < 9; ++q)
@@ -659,12 +685,18 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
   }
   if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
   collide<T, St::kShift>(d, m, k);
-  S* fout = (S*)a.fout;
+  // A special-first step keeps the results of cells in bulk columns in
+  // scratch for the bulk kernel; the first and last columns (never touched
+  // by the bulk kernel) go straight to the distributions.
+  const int i = cell / a.ny;
+  const bool to_buf = a.special_first && i > 0 && i < a.nx - 1;
+  S* dst = to_buf ? (S*)a.sbuf + s : (S*)a.fout + scell;
+  const long long stride = to_buf ? (long long)a.n_special : a.Ns;
   unsigned r = St::kStochastic ? sr_seed(scell, *a.it_dev) : 0u;
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
     if (St::kStochastic) r = xorshift32(r);
-    St::store_r(fout + q * a.Ns + scell, d[q], r);
+    St::store_r(dst + q * stride, d[q], r);
   }
 }
 

@@ -77,7 +77,16 @@ class _Replay:
 def run_fused(lattice, app, chunk=1000, graph=True, n_iter=None, verbose=True):
     """Fused-engine loop; returns the number of iterations run."""
     obstacles, walls, corners = trace_bc_program(app)
-    eng = FusedEngine(lattice, obstacles, walls, corners, drag_cap=chunk + 8)
+    # Apps that take a chunk of observables at once (observables_chunk) skip
+    # the per-iteration replay: their outputs act only at multiples of
+    # output_freq, and the hook evaluates check_stop itself.  With a known
+    # final iteration their chunks are replayed while the next chunk runs
+    # (the drag ring then holds two chunks).
+    chunk_obs = getattr(app, "observables_chunk", None)
+    known = getattr(app, "stop", None) == "it" and hasattr(app, "it_max")
+    overlap = chunk_obs is not None and (known or n_iter is not None)
+    eng = FusedEngine(lattice, obstacles, walls, corners,
+                      drag_cap=(2 * chunk if overlap else chunk) + 8)
     sched = app.bc_schedule(lattice) if hasattr(app, "bc_schedule") else None
     out_freq = getattr(app, "output_freq", None) or None
     known_stop = None
@@ -113,13 +122,10 @@ def run_fused(lattice, app, chunk=1000, graph=True, n_iter=None, verbose=True):
             eng.steps(first, last_it - first + 1, macro_last=macro_last, graph=use_graph)
 
     replay = _Replay(obstacles)
-    # Apps that take a chunk of observables at once (observables_chunk) skip
-    # the per-iteration replay: their outputs act only at multiples of
-    # output_freq, and the hook evaluates check_stop itself.
-    chunk_obs = getattr(app, "observables_chunk", None)
 
-    def replay_chunk(first, last_avail, honour_stop):
-        rows = eng.drag_rows(first, last_avail)
+    def replay_chunk(first, last_avail, honour_stop, rows=None):
+        if rows is None:
+            rows = eng.drag_rows(first, last_avail)
         if out_freq:
             m = max(first, state["outputs_done"] + 1)
             m = -(-m // out_freq) * out_freq
@@ -167,7 +173,41 @@ def run_fused(lattice, app, chunk=1000, graph=True, n_iter=None, verbose=True):
     state["outputs_done"] = 0
     last = 0      # last collided iteration: f[cur] = g_up(last)
     pending = 0   # first iteration whose observables/check_stop are pending
-    while known_stop is None or last < known_stop:
+    if overlap:
+        # chunk k + 1 is enqueued before chunk k's observables are replayed
+        # (on a side stream that waits only for chunk k)
+        side = torch.cuda.Stream()
+        queued = None  # (first, last iteration, event after its step)
+
+        def replay_queued(q):
+            rows = eng.drag_rows_after(q[0], q[1], q[2], side)
+            with torch.cuda.stream(side):
+                stop = replay_chunk(q[0], q[1], True, rows)
+            if stop is not None:
+                raise RuntimeError("check_stop stopped before the known final iteration")
+
+        while last < known_stop:
+            e = min(last + chunk, known_stop)
+            if out_freq:
+                e = min(e, (last // out_freq + 1) * out_freq)
+            steps(last + 1, e, macro_last=is_output(e) or e == known_stop, use_graph=graph)
+            ev = torch.cuda.Event()
+            ev.record()
+            if queued is not None:
+                replay_queued(queued)
+            queued = (pending, e - 1, ev)
+            if is_output(e):
+                ev.synchronize()
+                app.outputs(lattice, e)
+                state["outputs_done"] = e
+            pending = e
+            last = e
+            if verbose:
+                app.printings(e)
+        if queued is not None:
+            replay_queued(queued)
+        torch.cuda.synchronize()
+    while not overlap and (known_stop is None or last < known_stop):
         e = last + chunk
         if out_freq:
             e = min(e, (last // out_freq + 1) * out_freq)

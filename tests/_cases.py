@@ -78,8 +78,13 @@ def run_oracle(app, quiet=True):
     return lat, np.array(hist, dtype=np.float64).reshape(-1, 2)
 
 
-def run_gpu(app, fused=None, precision=None, chunk=1000, graph=True, quiet=True):
+def run_gpu(app, fused=None, precision=None, chunk=1000, graph=True, quiet=True, record=True):
+    """Run an app on the GPU lattice.  record: return the drag/lift series of
+    every lattice.drag_lift call (the app's per-iteration observables; an
+    app's chunked observables are turned off for that)."""
     import lbm_gb300
+    if record and getattr(app, "observables_chunk", None) is not None:
+        app.observables_chunk = None
     # The directory outlives the run: apps write their final files there.
     td = tempfile.mkdtemp(prefix="lbm_test_")
     with contextlib.redirect_stdout(io.StringIO() if quiet else None):

@@ -46,7 +46,9 @@ def test_add_chunk_matches_reference_goldens(cuda):
     assert b.obs == d["obs"][-1] and b.obs_cv == bool(d["cv"][-1])
     for k, ref in (("buff", d["buff"]), ("avg1_buff", d["avg1"]), ("avg2_buff", d["avg2"]),
                    ("avg3_buff", d["avg3"])):
-        assert np.array_equal(getattr(b, k), ref), k
+        got = getattr(b, k)
+        bad = np.flatnonzero(got != ref)
+        assert len(bad) == 0, (k, bad[:8], got[bad[:8]], ref[bad[:8]])
 
 
 def test_add_chunk_long_series_matches_host_buffer(cuda):
@@ -97,8 +99,8 @@ def test_turek_chunked_observables_match_per_iteration(cuda, stop):
     a = _turek(stop)
     b = _turek(stop)
     b.__class__ = type("turek_per_iteration", (_PerIteration, type(b)), {})
-    out_a, hist_a, lat_a = run_gpu(a, fused=True, chunk=128)
-    out_b, hist_b, lat_b = run_gpu(b, fused=True, chunk=128)
+    out_a, _, lat_a = run_gpu(a, fused=True, chunk=128, record=False)
+    out_b, _, lat_b = run_gpu(b, fused=True, chunk=128, record=False)
     with open(lat_a.output_dir + "drag_lift") as f:
         lines_a = f.read()
     with open(lat_b.output_dir + "drag_lift") as f:
