@@ -471,10 +471,10 @@ __device__ __forceinline__ void collide(T d[9], const Moments<T, SHIFT>& m, cons
 // ---------------------------------------------------------------------------
 // Two cells at once in packed FP32 (the FADD2 / FMUL2 / FFMA2 instructions of
 // sm_100 and later: one instruction for both elements of a float2).  Each
-// element goes through the operations of moments() and collide() on float;
-// the bulk kernels of the reduced forms, which update cells in pairs anyway
-// (packed conversions on store), use these to halve their FP32 instruction
-// count.
+// element goes through the arithmetic of moments() and collide() on float,
+// with w+ P +- M fused into one multiply-add; the bulk kernels of the
+// reduced forms, which update cells in pairs anyway (packed conversions on
+// store), use these to halve their FP32 instruction count.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -516,11 +516,10 @@ __device__ __forceinline__ void collide2(float2 d[9], const Moments2& m, const C
 #define LBM_PAIR2(q, qb, Q, cj, wp, wm)                                  \
   {                                                                      \
     const float2 P = fma2(f2(4.5f), Q, R);                               \
-    const float2 M = mul2(f2(wm), cj);                                   \
-    const float2 base = mul2(f2(wp), P);                                 \
+    const float2 M = mul2(f2(wm), cj), Mn = mul2(f2(-(wm)), cj);         \
     const float2 dq = d[q], dqb = d[qb];                                 \
-    d[q] = fma2(f2(k.a), dq, fma2(f2(k.mb), dqb, add2(base, M)));        \
-    d[qb] = fma2(f2(k.a), dqb, fma2(f2(k.mb), dq, sub2(base, M)));       \
+    d[q] = fma2(f2(k.a), dq, fma2(f2(k.mb), dqb, fma2(f2(wp), P, M)));   \
+    d[qb] = fma2(f2(k.a), dqb, fma2(f2(k.mb), dq, fma2(f2(wp), P, Mn))); \
   }
   LBM_PAIR2(1, 2, Qx, jx, k.wp1, k.wm1)
   LBM_PAIR2(3, 4, Qy, jy, k.wp1, k.wm1)

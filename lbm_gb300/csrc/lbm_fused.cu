@@ -91,7 +91,8 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
   // Special cells first (into scratch), then the bulk kernel, which stores
   // their values inside its whole-vector stores.
-  a.special_first = kUseVec && a.sy % kVec == 0 && with_special && a.special_mask ? 1 : 0;
+  a.special_first =
+      LBM_SPECIAL_FIRST && kUseVec && a.sy % kVec == 0 && with_special && a.special_mask ? 1 : 0;
   a.advance_at = with_drag ? 2 : (with_special && !a.special_first ? 1 : 0);
   if (ev) cudaEventRecord(ev[0], st);
   if (a.special_first) {
@@ -133,7 +134,8 @@ static void launch_store(const FusedArgs& a, int mode, cudaStream_t st, cudaEven
 }
 
 bool fused_special_first(const lbm_problem* p, int mode) {
-  if (mode != LBM_MODE_STEP || !p->special_mask || p->n_special <= 0) return false;
+  if (!LBM_SPECIAL_FIRST || mode != LBM_MODE_STEP || !p->special_mask || p->n_special <= 0)
+    return false;
   int elem = 0;
   switch (p->precision) {
     case LBM_PREC_F32: elem = 4; break;

@@ -260,6 +260,13 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
   const int j0 = valid ? (int)(gi - (long long)i * G) * V : 0;
   const bool active = valid && i > 0 && i < a.nx - 1;
   const unsigned lane = threadIdx.x & 31u;
+  // Special-first step: the group's special-cell bits (the group's V bits
+  // lie in one mask word: groups are V-aligned and V divides 32), loaded
+  // with the populations.
+  const long long c0 = (long long)i * sy + j0;
+  const unsigned sword = a.special_first && active ? __ldg(a.special_mask + (c0 >> 5)) : 0u;
+  const unsigned ssh = (unsigned)(c0 & 31);
+  const unsigned sbits = (sword >> ssh) & ((1u << V) - 1u);
   const S* fin = (const S*)a.fin;
   const Coef<T>& k = coef<T>(a);
 
@@ -320,14 +327,15 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
       }
       const Moments2 m = moments2<St::kShift>(d2, k.rho0, St::kInvScale);
       const int ja = j0 + e, jb = ja + 1;
+      // (special cells of a special-first step keep what k_special wrote)
       if (a.write_macro) {
-        if (ja < ny) {
+        if (ja < ny && !((sbits >> e) & 1u)) {
           const long long rc = (long long)i * ny + ja;
           a.rho_out[rc] = (double)m.rho.x;
           a.u_out[rc] = (double)m.ux.x;
           a.u_out[N + rc] = (double)m.uy.x;
         }
-        if (jb < ny) {
+        if (jb < ny && !((sbits >> (e + 1)) & 1u)) {
           const long long rc = (long long)i * ny + jb;
           a.rho_out[rc] = (double)m.rho.y;
           a.u_out[rc] = (double)m.ux.y;
@@ -372,7 +380,7 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
       }
       Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0, St::kInvScale);
       const int j = j0 + c;
-      if (j < ny && a.write_macro) {
+      if (j < ny && a.write_macro && !((sbits >> c) & 1u)) {
         const long long rc = (long long)i * ny + j;
         a.rho_out[rc] = (double)m.rho;
         a.u_out[rc] = (double)m.ux;
@@ -395,20 +403,15 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
     }
   }
   }
-  if (a.special_first) {
+  if (sbits) {
     // Special cells of this group: their values, computed by k_special into
-    // scratch, go into this group's vectors (the group's V bits lie in one
-    // mask word: groups are V-aligned and V divides 32).
-    const long long c0 = (long long)i * sy + j0;
-    const unsigned word = __ldg(a.special_mask + (c0 >> 5));
-    const unsigned sh = (unsigned)(c0 & 31);
-    const unsigned bits = (word >> sh) & ((1u << V) - 1u);
-    if (bits) {
-      int rank = __ldg(a.special_rank + (c0 >> 5)) + __popc(word & ((1u << sh) - 1u));
+    // scratch, go into this group's vectors.
+    {
+      int rank = __ldg(a.special_rank + (c0 >> 5)) + __popc(sword & ((1u << ssh) - 1u));
       const S* sb = (const S*)a.sbuf;
 #pragma unroll
       for (int c = 0; c < V; ++c) {
-        if ((bits >> c) & 1u) {
+        if ((sbits >> c) & 1u) {
 #pragma unroll
           for (int q = 0; q < 9; ++q) out[q].v[c] = sb[(long long)q * a.n_special + rank];
           ++rank;

@@ -15,7 +15,7 @@ from _cases import GOLDEN, make_case, run_gpu
 from lbm_gb300.buff import buff
 
 sys.path.insert(0, GOLDEN)
-from make_golden import BUFF_ARGS, buff_series  # noqa: E402
+from make_golden import BUFF_ARGS  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +35,7 @@ def test_add_chunk_matches_reference_goldens(cuda):
     d = np.load(os.path.join(GOLDEN, "buff.npz"))
     b = buff("drag", BUFF_ARGS["dt"], BUFF_ARGS["obs_cv_ct"], BUFF_ARGS["obs_cv_nb"], ".")
     obs, growth, cv = [], [], []
-    for part in _split(buff_series(), [1, 7, 300, 1200]):
+    for part in _split(d["buff"][2:], [1, 7, 300, 1200]):
         o, g, c = b.add_chunk(part)
         obs.append(o)
         growth.append(g)
