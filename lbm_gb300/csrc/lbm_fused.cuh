@@ -703,35 +703,30 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
   }
 }
 
-// Per-obstacle drag/lift: one block (256 threads) per obstacle, fixed-order
-// tree in FP64.
-__device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o) {
+// Per-obstacle drag/lift: one warp per obstacle, a fixed-order FP64 sum
+// (lane l adds links l, l + 32, ... in order, then a fixed shuffle tree), so
+// the result does not depend on scheduling.  Every lane of the warp calls it.
+__device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o, unsigned lane) {
   const double* link_force = a.link_force;
   const int n_links = a.n_links;
-  const int* obs_start = a.obs_start;
   long long slot = (*a.it_dev - 1) % a.drag_cap;
   if (slot < 0) slot += a.drag_cap;
-  double* out = a.drag_hist + slot * 2 * a.n_obs;
-  const int l0 = obs_start[o], l1 = obs_start[o + 1];
+  const int l0 = a.obs_start[o], l1 = a.obs_start[o + 1];
   double fx = 0.0, fy = 0.0;
-  for (int l = l0 + threadIdx.x; l < l1; l += blockDim.x) {
+#pragma unroll 4
+  for (int l = l0 + (int)lane; l < l1; l += 32) {
     fx += link_force[l];
     fy += link_force[n_links + l];
   }
-  __shared__ double sx[256], sy[256];
-  sx[threadIdx.x] = fx;
-  sy[threadIdx.x] = fy;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) {
-      sx[threadIdx.x] += sx[threadIdx.x + w];
-      sy[threadIdx.x] += sy[threadIdx.x + w];
-    }
-    __syncthreads();
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    fx += __shfl_down_sync(0xffffffffu, fx, off);
+    fy += __shfl_down_sync(0xffffffffu, fy, off);
   }
-  if (threadIdx.x == 0) {
-    out[2 * o] = sx[0];
-    out[2 * o + 1] = sy[0];
+  if (lane == 0) {
+    double* out = a.drag_hist + slot * 2 * a.n_obs;
+    out[2 * o] = fx;
+    out[2 * o + 1] = fy;
   }
 }
 
