@@ -70,7 +70,6 @@ extern "C" {
 #define LBM_MODE_STEP 1            /* stream+BC of f_in, then macro+eq+collide      */
 #define LBM_MODE_FINISH 2          /* stream+BC of f_in into g_out, no collision    */
 
-/* 2: lbm_problem carries special_mask / special_rank. */
 int lbm_abi_version(void);
 const char* lbm_last_error_string(void);
 /* Number of SMs and name of the current device (for logs/tuning). */
@@ -216,18 +215,6 @@ typedef struct lbm_problem {
    *             g[qb] = c1 g_up[q,x] + c2 g_up[qb,x] + c3 g_up[qb,x+c_qb]
    * (the factors of nb.py:98-104 in the reference's evaluation order). */
   const double* link_coef;
-
-  /* Special cells as a bitmask over the storage cells, for the shifted
-   * forms (optional, NULL: not used).  Bit c % 32 of special_mask[c / 32] is
-   * set when storage cell c = i * row_pitch + j is a special cell, and
-   * special_rank[w] is the number of special cells below storage cell 32 w
-   * (the special-cell table must then be sorted by linear index).  With
-   * them, a step of a shifted form runs the special-cell kernel first, into
-   * scratch, and the bulk kernel stores each special cell's values inside
-   * its own whole-vector stores, so that no kernel writes a part of a
-   * memory sector that another kernel writes. */
-  const uint32_t* special_mask;
-  const int32_t* special_rank;
 } lbm_problem;
 
 /* Flags for lbm_advance. */

@@ -67,7 +67,6 @@ class Problem(ctypes.Structure):
         ("rho_out", _vp), ("u_out", _vp), ("g_out", _vp), ("status_flags", _vp),
         ("row_pitch", _i32),
         ("link_coef", _vp),
-        ("special_mask", _vp), ("special_rank", _vp),
     ]
 
 

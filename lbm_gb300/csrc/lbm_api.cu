@@ -83,10 +83,6 @@ int problem_check(const lbm_problem* p, const char* fn) {
     set_error("%s: bad drag history", fn);
     return LBM_ERR_ARG;
   }
-  if (p->special_mask && !p->special_rank) {
-    set_error("%s: special_mask given without special_rank", fn);
-    return LBM_ERR_ARG;
-  }
   if (p->bc_vec && (!p->bc_scale || p->bc_scale_len <= 0)) {
     set_error("%s: bc_vec given without a scale table", fn);
     return LBM_ERR_ARG;
@@ -117,7 +113,7 @@ const size_t kMaxGraphs = 16;
 
 using namespace lbm;
 
-extern "C" int lbm_abi_version(void) { return 2; }
+extern "C" int lbm_abi_version(void) { return 1; }
 
 extern "C" const char* lbm_last_error_string(void) { return g_err; }
 
@@ -173,17 +169,13 @@ extern "C" int lbm_profile_steps(const lbm_problem* p, int64_t it0, int n_steps,
   }
   int rc = fused_enqueue(p, LBM_MODE_STEP, it0, n_steps, parity, flags, true, st, ev.data());
   double sums[3] = {0.0, 0.0, 0.0};
-  // The events bracket the kernels in launch order; slot[k] is the kernel
-  // (0 bulk, 1 special, 2 drag) of the k-th interval.
-  const bool sf = fused_special_first(p, LBM_MODE_STEP);
-  const int slot[3] = {sf ? 1 : 0, sf ? 0 : 1, 2};
   if (rc == LBM_OK) {
     cudaError_t err = cudaEventSynchronize(ev.back());
     for (int k = 0; k < n_steps && err == cudaSuccess; ++k) {
       for (int s = 0; s < 3 && err == cudaSuccess; ++s) {
         float ms = 0.f;
         err = cudaEventElapsedTime(&ms, ev[4 * k + s], ev[4 * k + s + 1]);
-        sums[slot[s]] += ms;
+        sums[s] += ms;
       }
     }
     if (err != cudaSuccess) {

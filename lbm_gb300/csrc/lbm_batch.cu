@@ -35,7 +35,6 @@ struct lbm_batch {
   unsigned* d_queue;        // [0] bulk queue, [1] special queue, [2] step-done count
   long long* d_it;          // shared iteration counter
   int any_scalar;
-  int special_first;        // special-cell kernel before the bulk kernel (see lbm_problem)
   // graph cache (one per (n_steps, parity))
   std::vector<int> g_steps, g_parity;
   std::vector<cudaGraphExec_t> g_exec;
@@ -160,24 +159,10 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
   const int gs = b->sm_count * b->cfg.special_blocks_per_sm;
   // The step's last kernel advances the shared iteration counter.
   const bool drag = b->n_drag_items > 0, special = b->n_special_tiles > 0;
-  const bool sf = b->special_first && special;
-  const int bulk_last = !drag && (sf || !special), special_last = !drag && special && !sf;
+  const int bulk_last = !drag && !special, special_last = !drag && special;
   for (int k = 0; k < n_steps; ++k) {
     const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
-    if (sf) {
-      // special cells into scratch, then the bulk tiles store them
-      if (b->cfg.persistent) {
-        k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
-                                                b->d_queue, b->d_it, 0);
-        k_batch_bulk<St, VB, kVecOnly><<<gb, b->cfg.bulk_threads, 0, st>>>(
-            args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
-      } else {
-        k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(
-            args, b->d_special_tiles, b->d_queue, b->d_it, 0);
-        k_batch_bulk_grid<St, VB, kVecOnly><<<b->n_bulk_tiles, b->cfg.bulk_threads, 0, st>>>(
-            args, b->d_bulk_tiles, b->d_queue, b->d_it, bulk_last);
-      }
-    } else if (b->cfg.persistent) {
+    if (b->cfg.persistent) {
       k_batch_bulk<St, VB, kVecOnly><<<gb, b->cfg.bulk_threads, 0, st>>>(
           args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
       if (special)
@@ -335,12 +320,6 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
   cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
   b->any_scalar = 0;
   for (const int4& t : bulk) b->any_scalar |= t.w == 0;
-  // Special-first steps when every lattice has its special-cell mask and
-  // every bulk tile is a vector tile.
-  b->special_first = b->any_scalar ? 0 : 1;
-  for (int c = 0; c < n_cases; ++c)
-    b->special_first &= fused_special_first(&cases[c], LBM_MODE_STEP) ? 1 : 0;
-  for (auto& a : args) a.special_first = b->special_first;
   b->n_bulk_tiles = (int)bulk.size();
   b->n_special_tiles = (int)special.size();
   b->n_drag_items = (int)drag.size();

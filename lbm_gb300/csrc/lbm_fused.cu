@@ -92,22 +92,8 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   // 16-byte vectors for the reduced storage forms (8 FP16/BF16 or 4 FP32 cells).
   constexpr int kVec = 16 / (int)sizeof(typename St::S);
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
-  // Special cells first (into scratch), then the bulk kernel, which stores
-  // their values inside its whole-vector stores.
-  a.special_first =
-      LBM_SPECIAL_FIRST && kUseVec && a.sy % kVec == 0 && with_special && a.special_mask ? 1 : 0;
-  a.advance_at = with_drag ? 2 : (with_special && !a.special_first ? 1 : 0);
+  a.advance_at = with_drag ? 2 : (with_special ? 1 : 0);
   if (ev) cudaEventRecord(ev[0], st);
-  if (a.special_first) {
-    k_special<St, MODE><<<(a.n_special + 127) / 128, 128, 0, st>>>(a);
-    if (ev) cudaEventRecord(ev[1], st);
-    const long long groups = (long long)a.nx * (a.sy / kVec);
-    k_bulk_vec<St, kVec><<<(unsigned)((groups + 127) / 128), 128, 0, st>>>(a);
-    if (ev) cudaEventRecord(ev[2], st);
-    if (with_drag) k_drag<<<(a.n_obs + 7) / 8, 256, 0, st>>>(a);
-    if (ev) cudaEventRecord(ev[3], st);
-    return;
-  }
   if (St::kFixed && MODE == LBM_MODE_STEP) {
     const int jb = (a.ny + 255) / 256;
     k_bulk_q60<<<(unsigned)((long long)a.nx * jb), 256, 0, st>>>(a, jb);
@@ -136,19 +122,6 @@ static void launch_store(const FusedArgs& a, int mode, cudaStream_t st, cudaEven
   }
 }
 
-bool fused_special_first(const lbm_problem* p, int mode) {
-  if (!LBM_SPECIAL_FIRST || mode != LBM_MODE_STEP || !p->special_mask || p->n_special <= 0)
-    return false;
-  int elem = 0;
-  switch (p->precision) {
-    case LBM_PREC_F32: elem = 4; break;
-    case LBM_PREC_F16S: case LBM_PREC_BF16S: case LBM_PREC_F16SR: case LBM_PREC_BF16SR: elem = 2; break;
-    default: return false;
-  }
-  const int sy = p->row_pitch > 0 ? p->row_pitch : p->ny;
-  return sy % (16 / elem) == 0;
-}
-
 int fused_kernels_per_step(const lbm_problem* p, int mode) {
   int n = 1 + (p->n_special > 0 ? 1 : 0);
   if (mode != LBM_MODE_COLLIDE_FROM_G && p->drag_hist && p->n_obstacles > 0 && p->n_links > 0) n++;
@@ -157,12 +130,11 @@ int fused_kernels_per_step(const lbm_problem* p, int mode) {
 
 // Scratch layout: iteration counter and step-done count (256 B) |
 // stale[2][9][n_special] | mac[2][3][n_special] | link_force[2][n_links]
-// (doubles) | special-cell results of a special-first step
-// [9][n_special] (storage elements, 4 bytes at most).
+// (doubles).
 size_t fused_scratch_bytes(const lbm_problem* p) {
   size_t ns = (size_t)(p->n_special > 0 ? p->n_special : 0);
   size_t nl = (size_t)(p->n_links > 0 ? p->n_links : 0);
-  return 256 + sizeof(double) * (2 * 9 * ns + 2 * 3 * ns + 2 * nl) + 4 * 9 * ns + 256;
+  return 256 + sizeof(double) * (2 * 9 * ns + 2 * 3 * ns + 2 * nl) + 256;
 }
 
 // Integer coefficients of the Q3.60 collision, rounded from the FP64 rates
@@ -230,10 +202,6 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.mac[0] = sc + 18 * ns;
   a.mac[1] = sc + 21 * ns;
   a.link_force = sc + 24 * ns;
-  a.sbuf = (void*)(sc + 24 * ns + 2 * (size_t)(p->n_links > 0 ? p->n_links : 0));
-  a.special_mask = p->special_mask;
-  a.special_rank = p->special_rank;
-  a.special_first = 0;
   a.drag_hist = p->drag_hist;
   a.drag_cap = p->drag_cap > 0 ? p->drag_cap : 1;
   a.n_obs = p->n_obstacles;

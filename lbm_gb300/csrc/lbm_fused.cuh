@@ -54,11 +54,6 @@ struct FusedArgs {
   double* stale[2];         // [9][n_special] post-BC g of an iteration
   double* mac[2];           // [3][n_special] macro rho, ux, uy of an iteration
   double* link_force;       // [2][n_links]
-  // special-first steps of the shifted forms (lbm_problem.special_mask)
-  const unsigned* special_mask;
-  const int* special_rank;
-  void* sbuf;               // [9][n_special] storage elements: special-cell results
-  int special_first;        // this launch runs k_special before the bulk kernel
   int n_links;
   // drag/lift history
   double* drag_hist;
@@ -260,13 +255,6 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
   const int j0 = valid ? (int)(gi - (long long)i * G) * V : 0;
   const bool active = valid && i > 0 && i < a.nx - 1;
   const unsigned lane = threadIdx.x & 31u;
-  // Special-first step: the group's special-cell bits (the group's V bits
-  // lie in one mask word: groups are V-aligned and V divides 32), loaded
-  // with the populations.
-  const long long c0 = (long long)i * sy + j0;
-  const unsigned sword = a.special_first && active ? __ldg(a.special_mask + (c0 >> 5)) : 0u;
-  const unsigned ssh = (unsigned)(c0 & 31);
-  const unsigned sbits = (sword >> ssh) & ((1u << V) - 1u);
   const S* fin = (const S*)a.fin;
   const Coef<T>& k = coef<T>(a);
 
@@ -327,15 +315,14 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
       }
       const Moments2 m = moments2<St::kShift>(d2, k.rho0, St::kInvScale);
       const int ja = j0 + e, jb = ja + 1;
-      // (special cells of a special-first step keep what k_special wrote)
       if (a.write_macro) {
-        if (ja < ny && !((sbits >> e) & 1u)) {
+        if (ja < ny) {
           const long long rc = (long long)i * ny + ja;
           a.rho_out[rc] = (double)m.rho.x;
           a.u_out[rc] = (double)m.ux.x;
           a.u_out[N + rc] = (double)m.uy.x;
         }
-        if (jb < ny && !((sbits >> (e + 1)) & 1u)) {
+        if (jb < ny) {
           const long long rc = (long long)i * ny + jb;
           a.rho_out[rc] = (double)m.rho.y;
           a.u_out[rc] = (double)m.ux.y;
@@ -380,7 +367,7 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
       }
       Moments<T, St::kShift> m = moments<T, St::kShift>(d, k.rho0, St::kInvScale);
       const int j = j0 + c;
-      if (j < ny && a.write_macro && !((sbits >> c) & 1u)) {
+      if (j < ny && a.write_macro) {
         const long long rc = (long long)i * ny + j;
         a.rho_out[rc] = (double)m.rho;
         a.u_out[rc] = (double)m.ux;
@@ -402,22 +389,6 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
       St::store_pair(&out[q].v[e], dd[0][q], dd[1][q], r);
     }
   }
-  }
-  if (sbits) {
-    // Special cells of this group: their values, computed by k_special into
-    // scratch, go into this group's vectors.
-    {
-      int rank = __ldg(a.special_rank + (c0 >> 5)) + __popc(sword & ((1u << ssh) - 1u));
-      const S* sb = (const S*)a.sbuf;
-#pragma unroll
-      for (int c = 0; c < V; ++c) {
-        if ((sbits >> c) & 1u) {
-#pragma unroll
-          for (int q = 0; q < 9; ++q) out[q].v[c] = sb[(long long)q * a.n_special + rank];
-          ++rank;
-        }
-      }
-    }
   }
   S* fout = (S*)a.fout;
 #pragma unroll
@@ -688,18 +659,12 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
   }
   if (a.check_finite && !isfinite(m.rho + m.ux + m.uy)) atomicOr(a.status, 1u);
   collide<T, St::kShift>(d, m, k);
-  // A special-first step keeps the results of cells in bulk columns in
-  // scratch for the bulk kernel; the first and last columns (never touched
-  // by the bulk kernel) go straight to the distributions.
-  const int i = cell / a.ny;
-  const bool to_buf = a.special_first && i > 0 && i < a.nx - 1;
-  S* dst = to_buf ? (S*)a.sbuf + s : (S*)a.fout + scell;
-  const long long stride = to_buf ? (long long)a.n_special : a.Ns;
+  S* fout = (S*)a.fout;
   unsigned r = St::kStochastic ? sr_seed(scell, *a.it_dev) : 0u;
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
     if (St::kStochastic) r = xorshift32(r);
-    St::store_r(dst + q * stride, d[q], r);
+    St::store_r(fout + q * a.Ns + scell, d[q], r);
   }
 }
 

@@ -14,13 +14,6 @@ size_t fused_scratch_bytes(const lbm_problem* p);
 int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, int parity,
                   unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev = nullptr);
 int fused_kernels_per_step(const lbm_problem* p, int mode);
-// True when a step of this problem runs the special-cell kernel before the
-// bulk kernel (shifted forms with special_mask: see lbm_problem).
-// LBM_SPECIAL_FIRST = 0 builds the library without that order.
-#ifndef LBM_SPECIAL_FIRST
-#define LBM_SPECIAL_FIRST 1
-#endif
-bool fused_special_first(const lbm_problem* p, int mode);
 int fused_set_it(const lbm_problem* p, long long value, cudaStream_t st);
 }  // namespace lbm
 

@@ -182,20 +182,6 @@ def build_tables(nx, ny, obstacles, ibb_on):
                 corner_nb_special=corner_nb)
 
 
-def special_mask(cells, n_cells):
-    """Bitmask and ranks of the special cells over the storage cells
-    (lbm_problem.special_mask / special_rank): bit c % 32 of word c // 32 is
-    set for each special cell c (storage index, ``cells`` sorted), and
-    rank[w] counts the special cells below 32 w, so the table index of
-    special cell c is rank[c // 32] + the set bits of its word below it."""
-    cells = np.asarray(cells, dtype=np.int64)
-    n_words = -(-int(n_cells) // 32)
-    words = np.zeros(n_words, np.uint32)
-    np.bitwise_or.at(words, cells >> 5, np.left_shift(np.uint32(1), (cells & 31).astype(np.uint32)))
-    rank = np.searchsorted(cells, 32 * np.arange(n_words, dtype=np.int64)).astype(np.int32)
-    return words, rank
-
-
 def ibb_coefficients(p):
     """[3][n] IBB coefficients of each link (lbm_problem.link_coef): the
     factors of the reference's interpolated bounce-back (nb.py:98-104),
@@ -269,15 +255,6 @@ class FusedEngine:
         self.t_obs_start = i32(np.array(starts))
         self.n_links = n_links
         self.n_special = n_special
-        # Shifted forms: special cells as a bitmask over the storage cells,
-        # so that a step runs the special-cell kernel first and the bulk
-        # kernel stores their values (lbm_problem.special_mask).
-        self.t_mask = self.t_rank = None
-        if self.precision not in ("f64", "q60") and n_special:
-            words, rank = special_mask(storage_index(special), nx * self.sy)
-            self.t_mask = torch.from_numpy(words.view(np.int32)).to(dev)
-            self._keep.append(self.t_mask)
-            self.t_rank = i32(rank)
 
         # ---- BC (packed) and schedule
         self.bc_base = torch.zeros(4 * ny + 4 * nx + ny, dtype=torch.float64, device=dev)
@@ -320,9 +297,6 @@ class FusedEngine:
         P.link_p = self.t_link_p.data_ptr()
         P.link_coef = self.t_link_coef.data_ptr()
         P.special_link_ids = self.t_link_ids.data_ptr()
-        if self.t_mask is not None:
-            P.special_mask = self.t_mask.data_ptr()
-            P.special_rank = self.t_rank.data_ptr()
         P.n_obstacles = len(self.obstacles)
         P.obstacle_link_start = self.t_obs_start.data_ptr()
         P.bc_base = self.bc_base.data_ptr()

@@ -9,7 +9,7 @@ import pytest
 
 from lbm_gb300 import _lib, geometry
 from lbm_gb300.apps import turek
-from lbm_gb300.engine import build_tables, ibb_coefficients, special_mask
+from lbm_gb300.engine import build_tables, ibb_coefficients
 
 CX = np.array([0, 1, -1, 0, 0, 1, -1, -1, 1])
 CY = np.array([0, 0, 0, 1, -1, 1, -1, 1, -1])
@@ -116,24 +116,3 @@ def test_links_leaving_the_lattice_are_refused():
     ob = types.SimpleNamespace(name="bad", boundary=np.array([[12, 3, 1]]), ibb=np.array([0.3]))
     with pytest.raises(IndexError):
         build_tables(10, 8, [ob], True)
-
-
-@pytest.mark.parametrize("case", list(_cases()), ids=lambda c: c[0])
-@pytest.mark.parametrize("pitch", [0, 8, 16])
-def test_special_mask_ranks_every_special_cell(case, pitch):
-    """special_mask / special_rank over the storage cells (rows padded to a
-    multiple of 8 or 16 cells, as the FP16/FP32 forms pad them): every
-    special cell's bit is set, no other bit is, and rank + the set bits
-    below a cell give its index in the special-cell table."""
-    _, nx, ny, obstacles, ibb = case
-    tb = build_tables(nx, ny, obstacles, ibb)
-    sy = ny if pitch == 0 else -(-ny // pitch) * pitch
-    cells = (tb["special"] // ny) * sy + tb["special"] % ny
-    words, rank = special_mask(cells, nx * sy)
-    assert len(words) == -(-nx * sy // 32)
-    bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:nx * sy].astype(bool)
-    assert np.array_equal(np.flatnonzero(bits), cells)
-    for s, c in enumerate(cells):
-        w = words[c >> 5]
-        below = bin(int(w) & ((1 << int(c & 31)) - 1)).count("1")
-        assert rank[c >> 5] + below == s
