@@ -21,7 +21,7 @@ stochastic rounding the run diverges, and with round to nearest it ran or
 diverged depending on how the FP32 arithmetic before the rounding was
 fused (one cell at a time: ran with mean Cd 1.8e-2 off FP64; two cells per
 packed instruction, the same operations per cell with w+ P +- M in one
-fused multiply-add: diverged near iteration 6,000).  At tau = 0.548 (the
+fused multiply-add: diverged within the 6,000 iterations).  At tau = 0.548 (the
 1100x200 channel of the benchmark's error study) both run.  The lattices have ny % 8 == 0, so the vectorised bulk
 kernel (16-byte loads, warp-shuffle halos) is the one tested.
 """
