@@ -458,6 +458,12 @@ def aligned_lag(ref, got, max_lag):
     return int(lags[np.argmax(c[lags % m] / (n - np.abs(lags)))])
 
 
+def smooth(x, w=101):
+    """Centred moving average over w iterations (w odd; the ends dropped)."""
+    c = np.cumsum(np.insert(np.asarray(x, dtype=np.float64), 0, 0.0))
+    return (c[w:] - c[:-w]) / w
+
+
 def series_errors(ref_cd, ref_cl, cd, cl, period):
     """Max deviation of the Cd / Cl series relative to the series' maximum
     magnitude, as they are and after shifting the form's series by the lag
@@ -489,7 +495,11 @@ def measure_form_errors(steps, forms, tmp, ny=200):
     over the second half of the run: mean Cd, rms Cl, max Cd, max Cl, the
     Cd oscillation amplitude and the shedding period; the whole Cd and Cl
     series (max deviation, as they are and phase-aligned); the velocity
-    field at the last iteration (L2).  Also returns the Cd/Cl series and
+    field at the last iteration (L2).  Amplitude, period, max Cl and the
+    series errors are also given on a 101-iteration moving average
+    ("_smoothed", about 2 % of the shedding period): the 16-bit forms' drag
+    and lift carry per-iteration rounding noise (a few 1e-2 of Cd) that the
+    raw extremes and zero crossings pick up.  Also returns the Cd/Cl series and
     final velocity of the two plain forms (f64, q60) for plain_vs_oracle."""
     import torch
     ref = run_channel("f64", ny, steps, tmp)
@@ -497,10 +507,13 @@ def measure_form_errors(steps, forms, tmp, ny=200):
 
     def stats(r):
         cd, cl = r["cd"][half], r["cl"][half]
+        cds, cls = smooth(cd), smooth(cl)
         return {"cd_mean": float(cd.mean()), "cl_rms": float(np.sqrt((cl ** 2).mean())),
                 "cd_max": float(cd.max()), "cl_max": float(cl.max()),
                 "cd_amplitude": float(0.5 * (cd.max() - cd.min())),
-                "period": shedding_period(cl)}
+                "period": shedding_period(cl),
+                "cd_amplitude_smoothed": float(0.5 * (cds.max() - cds.min())),
+                "cl_max_smoothed": float(cls.max()), "period_smoothed": shedding_period(cls)}
 
     sref = stats(ref)
     out = {"case": "cylinder channel %dx%d, D = %d, Re 100, %d iterations (all forms from the "
@@ -520,6 +533,9 @@ def measure_form_errors(steps, forms, tmp, ny=200):
         err["u_l2_rel"] = float(np.linalg.norm(r["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
         err.update(series_errors(ref["cd"][half], ref["cl"][half], r["cd"][half],
                                  r["cl"][half], sref["period"]))
+        sm = series_errors(smooth(ref["cd"][half]), smooth(ref["cl"][half]),
+                           smooth(r["cd"][half]), smooth(r["cl"][half]), sref["period_smoothed"])
+        err.update({k + "_smoothed": v for k, v in sm.items()})
         out[form] = dict(st, mlups=r["mlups"], error_vs_f64=err)
         del r
         torch.cuda.empty_cache()

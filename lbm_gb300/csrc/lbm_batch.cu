@@ -6,7 +6,7 @@
 //   k_batch_bulk     tiles of bulk cells of every lattice (16-byte vector
 //                    groups where ny % V == 0, single cells otherwise)
 //   k_batch_special  tiles of special cells of every lattice
-//   k_batch_drag     one warp per (lattice, obstacle)
+//   k_batch_drag     one block per (lattice, obstacle)
 //
 // The per-cell work is the single-lattice code of lbm_fused.cuh, reading the
 // lattice's FusedArgs from a device array (one array per ping-pong parity),
@@ -141,14 +141,13 @@ __global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_batch_special(c
   if (last) advance_counter(it_dev, queue + 2);
 }
 
-// One warp per (lattice, obstacle) item, eight per block.
+// One block of 256 threads per (lattice, obstacle) item.
 __global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict__ args,
                                                     const int2* __restrict__ items, int n_items,
                                                     unsigned* queue, long long* it_dev) {
-  const int w = blockIdx.x * 8 + (int)(threadIdx.x >> 5);
-  if (w < n_items) {
-    const int2 it = items[w];
-    drag_obstacle(args[it.x], it.y, threadIdx.x & 31u);
+  if ((int)blockIdx.x < n_items) {
+    const int2 it = items[blockIdx.x];
+    drag_obstacle(args[it.x], it.y);
   }
   advance_counter(it_dev, queue + 2);  // the drag kernel is always last
 }
@@ -176,8 +175,7 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
             args, b->d_special_tiles, b->d_queue, b->d_it, special_last);
     }
     if (drag)
-      k_batch_drag<<<(b->n_drag_items + 7) / 8, 256, 0, st>>>(args, b->d_drag_items,
-                                                              b->n_drag_items,
+      k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items,
                                                     b->d_queue, b->d_it);
   }
 }

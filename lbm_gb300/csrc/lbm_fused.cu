@@ -11,7 +11,7 @@
 //             sorted list): pull, links (IBB/BB), Zou-He walls in the app's
 //             order, corners, per-link drag terms, collide.  It overwrites
 //             what k_bulk wrote at link cells.
-//   k_drag    per obstacle (one warp each), a fixed-order FP64 sum of the
+//   k_drag    per obstacle (one block each), a fixed-order FP64 sum of the
 //             per-link terms.
 //
 // Edge populations without an in-domain source keep the previous post-BC
@@ -65,10 +65,9 @@ __global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_special(FusedAr
   if (a.advance_at == 1) advance_counter(a.it_dev, a.step_done);
 }
 
-// One warp per obstacle, eight per block.
+// One block of 256 threads per obstacle.
 __global__ void __launch_bounds__(256) k_drag(FusedArgs a) {
-  const int o = blockIdx.x * 8 + (int)(threadIdx.x >> 5);
-  if (o < a.n_obs) drag_obstacle(a, o, threadIdx.x & 31u);
+  if ((int)blockIdx.x < a.n_obs) drag_obstacle(a, blockIdx.x);
   if (a.advance_at == 2) advance_counter(a.it_dev, a.step_done);
 }
 
@@ -109,7 +108,7 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
     k_special<St, MODE><<<(a.n_special + ts - 1) / ts, ts, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[2], st);
-  if (with_drag) k_drag<<<(a.n_obs + 7) / 8, 256, 0, st>>>(a);
+  if (with_drag) k_drag<<<a.n_obs, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
 }
 

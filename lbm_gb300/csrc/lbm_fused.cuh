@@ -668,18 +668,18 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
   }
 }
 
-// Per-obstacle drag/lift: one warp per obstacle, a fixed-order FP64 sum
-// (lane l adds links l, l + 32, ... in order, then a fixed shuffle tree), so
-// the result does not depend on scheduling.  Every lane of the warp calls it.
-__device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o, unsigned lane) {
+// Per-obstacle drag/lift: one block of 256 threads per obstacle, a
+// fixed-order FP64 sum (thread t adds links t, t + 256, ... in order, each
+// warp reduces by a fixed shuffle tree, warp 0 adds the eight warp sums in
+// order), so the result does not depend on scheduling.
+__device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o) {
   const double* link_force = a.link_force;
   const int n_links = a.n_links;
   long long slot = (*a.it_dev - 1) % a.drag_cap;
   if (slot < 0) slot += a.drag_cap;
   const int l0 = a.obs_start[o], l1 = a.obs_start[o + 1];
   double fx = 0.0, fy = 0.0;
-#pragma unroll 4
-  for (int l = l0 + (int)lane; l < l1; l += 32) {
+  for (int l = l0 + (int)threadIdx.x; l < l1; l += blockDim.x) {
     fx += link_force[l];
     fy += link_force[n_links + l];
   }
@@ -688,10 +688,22 @@ __device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o, unsigne
     fx += __shfl_down_sync(0xffffffffu, fx, off);
     fy += __shfl_down_sync(0xffffffffu, fy, off);
   }
+  __shared__ double wx[8], wy[8];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   if (lane == 0) {
+    wx[warp] = fx;
+    wy[warp] = fy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sx = wx[0], sy = wy[0];
+    for (unsigned w = 1; w < (blockDim.x >> 5); ++w) {
+      sx += wx[w];
+      sy += wy[w];
+    }
     double* out = a.drag_hist + slot * 2 * a.n_obs;
-    out[2 * o] = fx;
-    out[2 * o + 1] = fy;
+    out[2 * o] = sx;
+    out[2 * o + 1] = sy;
   }
 }
 
