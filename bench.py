@@ -894,6 +894,12 @@ def main():
     if traffic and traffic.get(args.precision):
         tr = traffic[args.precision]
         roof["traffic"] = tr.get("bytes_per_launch")
+        roof["traffic_read"] = tr.get("read_bytes_per_launch")
+        roof["traffic_write"] = tr.get("write_bytes_per_launch")
+        alg = roof["bytes_per_unit"] * roof["units_per_launch"]
+        if roof["traffic_read"]:
+            # reads against the algorithmic reads (half the algorithmic bytes)
+            roof["read_over_algorithmic_read"] = roof["traffic_read"] / (alg / 2)
         roof["traffic_source"] = tr.get("source")
     roof["peak_source"] = peak_src
     dtype = {"q60": "int64", "f64": "f64", "f32": "f32", "f16s": "f16", "bf16s": "bf16",
