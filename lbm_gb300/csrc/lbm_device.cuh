@@ -164,19 +164,21 @@ __device__ __forceinline__ __nv_bfloat16 bf16_sr(float v, unsigned r) {
 // only its upper bits are used as dither.
 __device__ __forceinline__ unsigned lcg32(unsigned x) { return x * 1664525u + 1013904223u; }
 
-// Packed stochastic rounding of a pair (bulk kernel): dithers from one LCG
-// state, bits 19..31 and 6..18 for FP16; bits 16..31 and, after one more LCG
-// step, 16..31 for BF16.  No range check: the bulk values are deviations far
-// below the FP16 maximum, and below 2^-14 (FP16 subnormals) the dither is
-// smaller than the FP16 step, a bias below 6e-8.
-__device__ __forceinline__ unsigned f16x2_rz(float lo, float hi) {
+// Packed stochastic rounding in one instruction (cvt.rs, sm_100 and later):
+// the random bits rbits are added below the kept mantissa bits before
+// truncation, as the dither above, bits 0..12 for the low element and
+// 16..28 for the high one (FP16), 0..15 and 16..31 (BF16) -- the layout of
+// the instruction, confirmed on the GB300 with one bit set at a time on
+// values halfway between two neighbours.  The LCG's low bits are weak, so
+// the bulk kernels temper its state (r ^ r >> 15 or 16) first.
+__device__ __forceinline__ unsigned f16x2_rs(float lo, float hi, unsigned rbits) {
   unsigned d;
-  asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
   return d;
 }
-__device__ __forceinline__ unsigned bf16x2_rz(float lo, float hi) {
+__device__ __forceinline__ unsigned bf16x2_rs(float lo, float hi, unsigned rbits) {
   unsigned d;
-  asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
   return d;
 }
 
@@ -184,19 +186,14 @@ struct StoreF16SR : StoreF16 {
   static constexpr bool kStochastic = true;
   __device__ static void store_r(S* p, T v, unsigned r) { *p = half_sr(v, r); }
   __device__ static void store_pair(S* p, T v0, T v1, unsigned r) {
-    const float a = __uint_as_float(__float_as_uint(v0) + (r >> 19));
-    const float b = __uint_as_float(__float_as_uint(v1) + ((r >> 6) & 0x1fffu));
-    *reinterpret_cast<unsigned*>(p) = f16x2_rz(a, b);
+    *reinterpret_cast<unsigned*>(p) = f16x2_rs(v0, v1, r ^ (r >> 15));
   }
 };
 struct StoreBF16SR : StoreBF16 {
   static constexpr bool kStochastic = true;
   __device__ static void store_r(S* p, T v, unsigned r) { *p = bf16_sr(v, r); }
   __device__ static void store_pair(S* p, T v0, T v1, unsigned r) {
-    const unsigned r2 = lcg32(r);
-    const float a = __uint_as_float(__float_as_uint(v0) + (r >> 16));
-    const float b = __uint_as_float(__float_as_uint(v1) + (r2 >> 16));
-    *reinterpret_cast<unsigned*>(p) = bf16x2_rz(a, b);
+    *reinterpret_cast<unsigned*>(p) = bf16x2_rs(v0, v1, r ^ (r >> 16));
   }
 };
 
