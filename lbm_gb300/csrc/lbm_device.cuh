@@ -170,15 +170,10 @@ __device__ __forceinline__ unsigned lcg32(unsigned x) { return x * 1664525u + 10
 // 16..28 for the high one (FP16), 0..15 and 16..31 (BF16) -- the layout of
 // the instruction, confirmed on the GB300 with one bit set at a time on
 // values halfway between two neighbours.  The LCG's low bits are weak, so
-// the bulk kernels temper its state (r ^ r >> 15 or 16) first.
+// the FP16 bulk stores temper its state (r ^ r >> 15) first.
 __device__ __forceinline__ unsigned f16x2_rs(float lo, float hi, unsigned rbits) {
   unsigned d;
   asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
-  return d;
-}
-__device__ __forceinline__ unsigned bf16x2_rs(float lo, float hi, unsigned rbits) {
-  unsigned d;
-  asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
   return d;
 }
 
@@ -189,11 +184,23 @@ struct StoreF16SR : StoreF16 {
     *reinterpret_cast<unsigned*>(p) = f16x2_rs(v0, v1, r ^ (r >> 15));
   }
 };
+// BF16 pairs keep the dither: 16 random bits below the 7 kept mantissa bits
+// of each value (bits 16..31 of the state and of one more LCG step), then a
+// truncating packed conversion.  Measured on 8192x2048: 111.5 us per bulk
+// launch, against 127.1 us with bf16x2_rs.
+__device__ __forceinline__ unsigned bf16x2_rz(float lo, float hi) {
+  unsigned d;
+  asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
 struct StoreBF16SR : StoreBF16 {
   static constexpr bool kStochastic = true;
   __device__ static void store_r(S* p, T v, unsigned r) { *p = bf16_sr(v, r); }
   __device__ static void store_pair(S* p, T v0, T v1, unsigned r) {
-    *reinterpret_cast<unsigned*>(p) = bf16x2_rs(v0, v1, r ^ (r >> 16));
+    const unsigned r2 = lcg32(r);
+    const float a = __uint_as_float(__float_as_uint(v0) + (r >> 16));
+    const float b = __uint_as_float(__float_as_uint(v1) + (r2 >> 16));
+    *reinterpret_cast<unsigned*>(p) = bf16x2_rz(a, b);
   }
 };
 
