@@ -23,8 +23,6 @@
 #include <math.h>
 #include <string.h>
 
-#include <mutex>
-
 namespace lbm {
 
 template <class St, int MODE>
@@ -92,42 +90,6 @@ __global__ void k_set_it(long long* it_dev, unsigned* done, long long value) {
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-// Side stream and fork/join events of the current device for the link-group
-// kernel.  Created by a launch outside stream capture (fused_enqueue);
-// until then (a first launch inside a capture) the kernels run one after
-// the other on the caller's stream.
-struct StepStreams {
-  cudaStream_t side;
-  cudaEvent_t fork, join;
-};
-static std::mutex g_ss_mu;
-static StepStreams* g_ss[64] = {};
-static thread_local StepStreams* t_ss = nullptr;  // set by fused_enqueue for its launches
-
-static StepStreams* step_streams() { return t_ss; }
-
-static StepStreams* prepare_step_streams(cudaStream_t st) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lk(g_ss_mu);
-  if (g_ss[dev]) return g_ss[dev];
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
-    return nullptr;
-  StepStreams* s = new StepStreams();
-  if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess) {
-    delete s;
-    return nullptr;
-  }
-  if (cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess) {
-    cudaStreamDestroy(s->side);
-    delete s;
-    return nullptr;
-  }
-  g_ss[dev] = s;
-  return s;
-}
 // ev (optional): four events recorded before k_bulk, k_special (with
 // k_link_groups), k_drag and after the step, for per-kernel timing.
 template <class St, int MODE>
@@ -154,26 +116,12 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
     k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[1], st);
-  const size_t group_smem = 9 * (size_t)a.group_max_slots * sizeof(typename St::S);
-  // The per-cell kernel and the link groups (disjoint cells) run side by
-  // side when a side stream is at hand and the drag kernel, which joins
-  // them, advances the counter.
-  StepStreams* ss = with_groups && with_drag ? step_streams() : nullptr;
-  if (ss) {
-    cudaEventRecord(ss->fork, st);
-    cudaStreamWaitEvent(ss->side, ss->fork, 0);
-    k_link_groups<St><<<a.n_groups, 256, group_smem, ss->side>>>(a);
-    cudaEventRecord(ss->join, ss->side);
-  }
   if (with_special && n_cells > 0) {
     const int ts = 128;
     k_special<St, MODE><<<(n_cells + ts - 1) / ts, ts, 0, st>>>(a, n_cells);
   }
-  if (ss) {
-    cudaStreamWaitEvent(st, ss->join, 0);
-  } else if (with_groups) {
-    k_link_groups<St><<<a.n_groups, 256, group_smem, st>>>(a);
-  }
+  if (with_groups)
+    k_link_groups<St><<<a.n_groups, 256, 9 * a.group_max_slots * sizeof(typename St::S), st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
   if (with_drag) k_drag<<<a.n_obs, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
@@ -297,7 +245,6 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
 int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, int parity,
                   unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev) {
   FusedArgs a = make_args(p, mode, flags);
-  t_ss = p->n_link_groups > 0 ? prepare_step_streams(st) : nullptr;
   if (set_it) k_set_it<<<1, 1, 0, st>>>(a.it_dev, a.step_done, it0);
   for (int k = 0; k < n_steps; ++k) {
     const int par = (parity + k) & 1;  // f[par] holds g_up of the previous iteration

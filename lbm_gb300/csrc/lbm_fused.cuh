@@ -678,8 +678,8 @@ __device__ __forceinline__ void special_finish(const FusedArgs& a, int s, int i,
 // Staged link cells (LBM_MODE_STEP): one block per link group (the pure
 // link cells of one obstacle, lbm_problem).  The nine populations of every
 // cell the group's pulls and IBB stencils read are copied into shared
-// memory first (consecutive threads on consecutive staged cells, the nine
-// loads of a cell independent), and each cell then takes its
+// memory first -- all loads of the block in flight at once, consecutive
+// threads on consecutive staged cells -- and each cell then takes its
 // pulls and stencil values from there; the links, the drag terms and the
 // rest of the step are the per-cell kernel's code (ibb_combine, link_term,
 // special_finish), so a cell gets the same bits from either kernel.
@@ -690,15 +690,9 @@ __device__ __forceinline__ void link_group(const FusedArgs& a, int g, typename S
   const int s0 = a.group_slot_start[g], ns = a.group_slot_start[g + 1] - s0;
   const S* fin = (const S*)a.fin;
   const long long Ns = a.Ns;
-  // one staged cell per thread and round: its index, then its nine
-  // populations (independent loads)
-  for (int kk = threadIdx.x; kk < ns; kk += blockDim.x) {
-    const long long c = __ldg(a.slot_cell + s0 + kk);
-    S v[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) v[q] = fin[(long long)q * Ns + c];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) sm[q * ns + kk] = v[q];
+  for (int e = threadIdx.x; e < 9 * ns; e += blockDim.x) {
+    const int q = e / ns, kk = e - q * ns;
+    sm[e] = fin[(long long)q * Ns + __ldg(a.slot_cell + s0 + kk)];
   }
   __syncthreads();
   const T rho0 = St::kShift ? T(a.kd.rho0) : T(0);
