@@ -70,7 +70,6 @@ extern "C" {
 #define LBM_MODE_STEP 1            /* stream+BC of f_in, then macro+eq+collide      */
 #define LBM_MODE_FINISH 2          /* stream+BC of f_in into g_out, no collision    */
 
-/* 2: lbm_problem carries the link groups. */
 int lbm_abi_version(void);
 const char* lbm_last_error_string(void);
 /* Number of SMs and name of the current device (for logs/tuning). */
@@ -216,28 +215,6 @@ typedef struct lbm_problem {
    *             g[qb] = c1 g_up[q,x] + c2 g_up[qb,x] + c3 g_up[qb,x+c_qb]
    * (the factors of nb.py:98-104 in the reference's evaluation order). */
   const double* link_coef;
-
-  /* Link groups (optional; n_link_groups = 0: the per-cell kernel takes every
-   * special cell).  Special cells n_special_main .. n_special - 1 are the
-   * link cells of obstacles that lie off the walls and whose links all
-   * belong to one obstacle, in groups: group g is cells group_cell_start[g]
-   * .. group_cell_start[g + 1] - 1 (group_cell_start[0] = n_special_main,
-   * the last entry n_special).  A step updates each group in one block that
-   * first copies the nine populations of the group's staged cells (storage
-   * indices slot_cell[group_slot_start[g] .. group_slot_start[g + 1] - 1])
-   * into shared memory.  pull_slot[9 (s - n_special_main) + q] is the slot,
-   * within its group, of cell s's pull source x - c_q; link_slot[2 k] and
-   * [2 k + 1] are the slots of link k's IBB stencil cells (x + c_qb and
-   * x + 2 c_qb when p < 1/2, else x and x + c_qb).  9 * group_max_slots
-   * storage elements must fit in 48 KB. */
-  int32_t n_special_main;
-  int32_t n_link_groups;
-  const int32_t* group_cell_start;
-  const int32_t* group_slot_start;
-  const int32_t* slot_cell;
-  const int32_t* pull_slot;
-  const int32_t* link_slot;
-  int32_t group_max_slots;
 } lbm_problem;
 
 /* Flags for lbm_advance. */

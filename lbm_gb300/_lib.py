@@ -67,9 +67,6 @@ class Problem(ctypes.Structure):
         ("rho_out", _vp), ("u_out", _vp), ("g_out", _vp), ("status_flags", _vp),
         ("row_pitch", _i32),
         ("link_coef", _vp),
-        ("n_special_main", _i32), ("n_link_groups", _i32), ("group_cell_start", _vp),
-        ("group_slot_start", _vp), ("slot_cell", _vp), ("pull_slot", _vp), ("link_slot", _vp),
-        ("group_max_slots", _i32),
     ]
 
 

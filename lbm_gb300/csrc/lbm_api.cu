@@ -83,23 +83,6 @@ int problem_check(const lbm_problem* p, const char* fn) {
     set_error("%s: bad drag history", fn);
     return LBM_ERR_ARG;
   }
-  if (p->n_link_groups < 0 ||
-      (p->n_link_groups > 0 &&
-       (p->n_special_main < 1 || p->n_special_main > p->n_special || !p->group_cell_start ||
-        !p->group_slot_start || !p->slot_cell || !p->pull_slot || p->group_max_slots < 1 ||
-        (p->n_links > 0 && p->ibb && !p->link_slot)))) {
-    set_error("%s: bad link-group tables", fn);
-    return LBM_ERR_ARG;
-  }
-  if (p->n_link_groups > 0) {
-    const int elem = p->precision == LBM_PREC_F64 || p->precision == LBM_PREC_Q60 ? 8
-                     : p->precision == LBM_PREC_F32 ? 4 : 2;
-    if ((long long)9 * p->group_max_slots * elem > 48 * 1024) {
-      set_error("%s: link group of %d staged cells exceeds 48 KB of shared memory", fn,
-                p->group_max_slots);
-      return LBM_ERR_ARG;
-    }
-  }
   if (p->bc_vec && (!p->bc_scale || p->bc_scale_len <= 0)) {
     set_error("%s: bc_vec given without a scale table", fn);
     return LBM_ERR_ARG;
@@ -130,7 +113,7 @@ const size_t kMaxGraphs = 16;
 
 using namespace lbm;
 
-extern "C" int lbm_abi_version(void) { return 2; }
+extern "C" int lbm_abi_version(void) { return 1; }
 
 extern "C" const char* lbm_last_error_string(void) { return g_err; }
 

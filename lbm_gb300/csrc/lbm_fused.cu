@@ -58,25 +58,14 @@ __global__ void __launch_bounds__(256, LBM_Q60_MIN_BLOCKS) k_bulk_q60(FusedArgs 
   if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
-// n_cells: a.n_main in a step with link groups (their cells are k_link_groups'),
-// else a.n_special.
 template <class St, int MODE>
-__global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_special(FusedArgs a, int n_cells) {
+__global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_special(FusedArgs a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n_cells) special_cell<St, MODE>(a, s);
+  if (s < a.n_special) special_cell<St, MODE>(a, s);
   if (a.advance_at == 1) advance_counter(a.it_dev, a.step_done);
 }
 
 // One block of 256 threads per obstacle.
-// One block per link group; dynamic shared memory: 9 x group_max_slots
-// storage elements (48 KB at most, lbm_problem).
-template <class St>
-__global__ void __launch_bounds__(256) k_link_groups(FusedArgs a) {
-  extern __shared__ __align__(16) unsigned char lg_smem[];
-  link_group<St>(a, blockIdx.x, reinterpret_cast<typename St::S*>(lg_smem));
-  if (a.advance_at == 3) advance_counter(a.it_dev, a.step_done);
-}
-
 __global__ void __launch_bounds__(256) k_drag(FusedArgs a) {
   if ((int)blockIdx.x < a.n_obs) drag_obstacle(a, blockIdx.x);
   if (a.advance_at == 2) advance_counter(a.it_dev, a.step_done);
@@ -90,21 +79,19 @@ __global__ void k_set_it(long long* it_dev, unsigned* done, long long value) {
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-// ev (optional): four events recorded before k_bulk, k_special (with
-// k_link_groups), k_drag and after the step, for per-kernel timing.
+// ev (optional): four events recorded before k_bulk, k_special, k_drag and
+// after the step, for per-kernel timing.
 template <class St, int MODE>
 static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   FusedArgs a = a0;
   const bool with_special = a.n_special > 0;
   const bool with_drag = MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0;
-  const bool with_groups = MODE == LBM_MODE_STEP && a.n_groups > 0;
-  const int n_cells = with_groups ? a.n_main : a.n_special;
   const int tb = 256;
   const long long nb = (a.Ns + tb - 1) / tb;
   // 16-byte vectors for the reduced storage forms (8 FP16/BF16 or 4 FP32 cells).
   constexpr int kVec = 16 / (int)sizeof(typename St::S);
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
-  a.advance_at = with_drag ? 2 : (with_groups ? 3 : (with_special ? 1 : 0));
+  a.advance_at = with_drag ? 2 : (with_special ? 1 : 0);
   if (ev) cudaEventRecord(ev[0], st);
   if (St::kFixed && MODE == LBM_MODE_STEP) {
     const int jb = (a.ny + 255) / 256;
@@ -116,12 +103,10 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
     k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[1], st);
-  if (with_special && n_cells > 0) {
+  if (with_special) {
     const int ts = 128;
-    k_special<St, MODE><<<(n_cells + ts - 1) / ts, ts, 0, st>>>(a, n_cells);
+    k_special<St, MODE><<<(a.n_special + ts - 1) / ts, ts, 0, st>>>(a);
   }
-  if (with_groups)
-    k_link_groups<St><<<a.n_groups, 256, 9 * a.group_max_slots * sizeof(typename St::S), st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
   if (with_drag) k_drag<<<a.n_obs, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
@@ -138,7 +123,6 @@ static void launch_store(const FusedArgs& a, int mode, cudaStream_t st, cudaEven
 
 int fused_kernels_per_step(const lbm_problem* p, int mode) {
   int n = 1 + (p->n_special > 0 ? 1 : 0);
-  if (mode == LBM_MODE_STEP && p->n_link_groups > 0) n++;
   if (mode != LBM_MODE_COLLIDE_FROM_G && p->drag_hist && p->n_obstacles > 0 && p->n_links > 0) n++;
   return n;
 }
@@ -207,14 +191,6 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.link_p = p->link_p;
   a.link_coef = p->link_coef;
   a.n_links = p->n_links;
-  a.n_groups = p->n_link_groups;
-  a.n_main = p->n_link_groups > 0 ? p->n_special_main : p->n_special;
-  a.group_cell_start = p->group_cell_start;
-  a.group_slot_start = p->group_slot_start;
-  a.slot_cell = p->slot_cell;
-  a.pull_slot = p->pull_slot;
-  a.link_slot = p->link_slot;
-  a.group_max_slots = p->group_max_slots;
   char* base = (char*)(((uintptr_t)p->scratch + 255) & ~(uintptr_t)255);
   a.it_dev = (long long*)base;
   a.step_done = (unsigned*)(base + 8);

@@ -54,15 +54,6 @@ struct FusedArgs {
   double* stale[2];         // [9][n_special] post-BC g of an iteration
   double* mac[2];           // [3][n_special] macro rho, ux, uy of an iteration
   double* link_force;       // [2][n_links]
-  // link groups (lbm_problem): staged link cells, s in [n_main, n_special)
-  int n_main;               // special cells of the per-cell kernel in a STEP launch
-  int n_groups;
-  const int* group_cell_start;
-  const int* group_slot_start;
-  const int* slot_cell;
-  const int* pull_slot;
-  const int* link_slot;
-  int group_max_slots;
   int n_links;
   // drag/lift history
   double* drag_hist;
@@ -430,31 +421,6 @@ __device__ __forceinline__ bool is_corner_neighbour(const FusedArgs& a, int s) {
   return r;
 }
 
-// IBB coefficients of link k (the host's link_coef, or from p), and the
-// interpolated value: p < 1/2: c1 f_q(x) + c2 f_q(x1) - c3 f_q(x2); else
-// c1 f_q(x) + c2 f_qb(x) + c3 f_qb(x1) (u1, u2 the two stencil values).
-// Shared by the per-cell and the staged link kernels, so that a cell gets
-// the same bits from either.
-template <typename T>
-__device__ __forceinline__ void link_coefs(const FusedArgs& a, int k, T p, T& c1, T& c2, T& c3) {
-  if (a.link_coef) {
-    c1 = (T)a.link_coef[k];
-    c2 = (T)a.link_coef[a.n_links + k];
-    c3 = (T)a.link_coef[2 * a.n_links + k];
-  } else {
-    ibb_coefs<T>(p, c1, c2, c3);
-  }
-}
-template <typename T>
-__device__ __forceinline__ T ibb_combine(bool near, T c1, T c2, T c3, T up, T u1, T u2) {
-  return c1 * up + c2 * u1 + (near ? -c3 : c3) * u2;
-}
-// Momentum-exchange term of a link (nb.py:49-73) in FP64.
-template <typename T>
-__device__ __forceinline__ double link_term(T up, T g_qb) {
-  return (double)up + (double)g_qb;
-}
-
 // Post-BC state of special cell s without corners (pull, links, wall ops),
 // in the storage form's arithmetic type T (FP64 for the plain form, FP32 for
 // the reduced forms).
@@ -502,15 +468,22 @@ __device__ void bc_chain(const FusedArgs& a, long long it, int s, CellBC<typenam
       const T p = (T)a.link_p[k];
       const long long x1 = a.link_nb1[k];
       T c1, c2, c3;
-      link_coefs<T>(a, k, p, c1, c2, c3);
-      // One load pattern for both branches (ibb_combine).
+      if (a.link_coef) {
+        c1 = (T)a.link_coef[k];
+        c2 = (T)a.link_coef[a.n_links + k];
+        c3 = (T)a.link_coef[2 * a.n_links + k];
+      } else {
+        ibb_coefs<T>(p, c1, c2, c3);
+      }
+      // p < 1/2: c1 f_q(x) + c2 f_q(x1) - c3 f_q(x2);
+      // else:    c1 f_q(x) + c2 f_qb(x) + c3 f_qb(x1).  One load pattern.
       const bool near = p < T(0.5);
       const int qy = near ? q : qb;
       const long long y1 = qy * Ns + (near ? x1 : x);
       const long long y2 = qy * Ns + (near ? a.link_nb2[k] : x1);
       const T u1 = full_value<St>(fin + y1, qy, rho0);
       const T u2 = full_value<St>(fin + y2, qy, rho0);
-      v = ibb_combine<T>(near, c1, c2, c3, up_q_x, u1, u2);
+      v = c1 * up_q_x + c2 * u1 + (near ? -c3 : c3) * u2;
     }
     set_pop<T>(c.g, qb, v);
   }
@@ -558,10 +531,6 @@ __device__ __forceinline__ bool on_wall_op(const FusedArgs& a, int i, int j) {
 template <class St>
 __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int cell,
                                                 long long scell, CellBC<typename St::T>& c);
-template <class St>
-__device__ __forceinline__ void special_finish(const FusedArgs& a, int s, int i, int j, int cell,
-                                               long long scell, long long it,
-                                               CellBC<typename St::T>& c);
 
 template <class St, int MODE>
 __device__ __forceinline__ void special_cell(const FusedArgs& a, int s) {
@@ -597,7 +566,7 @@ __device__ __forceinline__ void special_cell(const FusedArgs& a, int s) {
       const int kk = a.special_link_ids[l];
       const int q = a.link_q[kk];
       const double g0 =
-          link_term<T>(full_value<St>(fin + q * a.Ns + scell, q, rho0), get_pop<T>(c.g, opp(q)));
+          (double)full_value<St>(fin + q * a.Ns + scell, q, rho0) + (double)get_pop<T>(c.g, opp(q));
       a.link_force[kk] = g0 * (double)cx(q);
       a.link_force[a.n_links + kk] = g0 * (double)cy(q);
     }
@@ -614,18 +583,6 @@ __device__ __forceinline__ void special_cell(const FusedArgs& a, int s) {
       return;
     }
   }
-  special_finish<St>(a, s, i, j, cell, scell, it, c);
-}
-
-// Everything of a special cell's step after its boundary operations: the
-// populations its next pull cannot reach (walls only), the macro values a
-// corner reads, the collision and the store.
-template <class St>
-__device__ __forceinline__ void special_finish(const FusedArgs& a, int s, int i, int j, int cell,
-                                               long long scell, long long it,
-                                               CellBC<typename St::T>& c) {
-  const long long N = a.N;
-  const int ny = a.ny;
   // Keep the post-BC value of the populations the next iteration cannot pull
   // (sources outside the lattice: only on walls).
   double* stale_out = a.stale[it & 1];
@@ -672,75 +629,6 @@ __device__ __forceinline__ void special_finish(const FusedArgs& a, int s, int i,
     for (int q = 0; q < 9; ++q) fout[q * a.Ns + scell] = x[q];
   } else {
     special_collide<St>(a, s, cell, scell, c);
-  }
-}
-
-// Staged link cells (LBM_MODE_STEP): one block per link group (the pure
-// link cells of one obstacle, lbm_problem).  The nine populations of every
-// cell the group's pulls and IBB stencils read are copied into shared
-// memory first -- all loads of the block in flight at once, consecutive
-// threads on consecutive staged cells -- and each cell then takes its
-// pulls and stencil values from there; the links, the drag terms and the
-// rest of the step are the per-cell kernel's code (ibb_combine, link_term,
-// special_finish), so a cell gets the same bits from either kernel.
-template <class St>
-__device__ __forceinline__ void link_group(const FusedArgs& a, int g, typename St::S* sm) {
-  using S = typename St::S;
-  using T = typename St::T;
-  const int s0 = a.group_slot_start[g], ns = a.group_slot_start[g + 1] - s0;
-  const S* fin = (const S*)a.fin;
-  const long long Ns = a.Ns;
-  for (int e = threadIdx.x; e < 9 * ns; e += blockDim.x) {
-    const int q = e / ns, kk = e - q * ns;
-    sm[e] = fin[(long long)q * Ns + __ldg(a.slot_cell + s0 + kk)];
-  }
-  __syncthreads();
-  const T rho0 = St::kShift ? T(a.kd.rho0) : T(0);
-  const long long it = *a.it_dev;
-  const int c0 = a.group_cell_start[g], c1 = a.group_cell_start[g + 1];
-  for (int s = c0 + (int)threadIdx.x; s < c1; s += blockDim.x) {
-    const int cell = a.special_cell[s];
-    const int i = cell / a.ny, j = cell - i * a.ny;
-    const long long scell = (long long)i * a.sy + j;
-    const int* ps = a.pull_slot + 9LL * (s - a.n_main);
-    CellBC<T> c;
-    int sl[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) sl[q] = __ldg(ps + q);
-#pragma unroll
-    for (int q = 0; q < 9; ++q) c.g[q] = full_value<St>(sm + q * ns + sl[q], q, rho0);
-    c.rho = c.ux = c.uy = T(0);  // not read: a group cell is never a corner's neighbour
-    // Obstacle links, in reference order (nb.py:77-117); x is the cell itself
-    // (pull slot of q = 0).
-    const int own = sl[0];
-    const int l0 = a.special_link_start[s], l1 = a.special_link_start[s + 1];
-    for (int l = l0; l < l1; ++l) {
-      const int k = a.special_link_ids[l];
-      const int q = a.link_q[k], qb = opp(q);
-      const T up = full_value<St>(sm + q * ns + own, q, rho0);
-      T v = up;
-      if (a.ibb) {
-        const T p = (T)a.link_p[k];
-        T cc1, cc2, cc3;
-        link_coefs<T>(a, k, p, cc1, cc2, cc3);
-        const bool near = p < T(0.5);
-        const int qy = near ? q : qb;
-        const T u1 = full_value<St>(sm + qy * ns + __ldg(a.link_slot + 2 * k), qy, rho0);
-        const T u2 = full_value<St>(sm + qy * ns + __ldg(a.link_slot + 2 * k + 1), qy, rho0);
-        v = ibb_combine<T>(near, cc1, cc2, cc3, up, u1, u2);
-      }
-      set_pop<T>(c.g, qb, v);
-    }
-    // Per-link momentum exchange terms (nb.py:49-73).
-    for (int l = l0; l < l1; ++l) {
-      const int k = a.special_link_ids[l];
-      const int q = a.link_q[k];
-      const double g0 = link_term<T>(full_value<St>(sm + q * ns + own, q, rho0),
-                                     get_pop<T>(c.g, opp(q)));
-      a.link_force[k] = g0 * (double)cx(q);
-      a.link_force[a.n_links + k] = g0 * (double)cy(q);
-    }
-    special_finish<St>(a, s, i, j, cell, scell, it, c);
   }
 }
 

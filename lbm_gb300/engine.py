@@ -182,104 +182,6 @@ def build_tables(nx, ny, obstacles, ibb_on):
                 corner_nb_special=corner_nb)
 
 
-def link_groups(tb, nx, ny, sy, ibb_on, elem_bytes, smem_cap=48 * 1024):
-    """Tables of the staged link-cell kernel (lbm_problem link groups).
-
-    A group is the link cells of one obstacle that lie off the walls and
-    whose links all belong to that obstacle ("pure" link cells).  Its
-    staged cells are every storage cell the group's pulls (x - c_q, q = 0..8)
-    and IBB stencils (link_nb1 / link_nb2 of its links) read; a block copies
-    their nine populations into shared memory once and updates the group's
-    cells from there.  ``smem_cap``: the shared memory a block may use
-    (48 KB: no opt-in attribute needed).
-
-    Returns the special-cell table reordered so that the per-cell kernel's
-    cells come first (in their original order) and each group's cells
-    follow, with the CSR link lists and corner indices of that order, and
-    the group tables: group_cell_start (special-index ranges),
-    group_slot_start (ranges into slot_cell), slot_cell (storage index of
-    each staged cell), pull_slot ([n_group_cells][9], slot of each pull
-    source within its group), link_slot ([n_links][2], slots of each link's
-    IBB sources; -1 outside the groups).
-    """
-    special, ls, ids = tb["special"], tb["link_start"], tb["link_ids"]
-    n_special, n_links = len(special), tb["n_links"]
-    ci, cj = special // ny, special % ny
-    n_cell_links = np.diff(ls)
-    obs_of_link = (np.searchsorted(tb["obs_start"], np.arange(n_links), side="right") - 1
-                   if n_links else np.zeros(0, np.int64))
-    cell_obs = np.full(n_special, -1, np.int64)
-    same = np.zeros(n_special, bool)
-    has = n_cell_links > 0
-    if n_links:
-        ob = obs_of_link[ids]
-        starts = ls[:-1][has]
-        lo = np.minimum.reduceat(ob, starts)
-        hi = np.maximum.reduceat(ob, starts)
-        cell_obs[has] = lo
-        same[has] = lo == hi
-    pure = has & same & (ci >= 1) & (ci <= nx - 2) & (cj >= 1) & (cj <= ny - 2)
-
-    def storage(ref):
-        ref = np.asarray(ref, np.int64)
-        return (ref // ny) * sy + ref % ny
-
-    groups, slots_all, pull_rows, link_slot = [], [], [], np.full((max(n_links, 1), 2), -1, np.int64)
-    in_group = np.zeros(n_special, bool)
-
-    def add_group(cells):
-        pulls = ((ci[cells, None] - _CX[None, :]) * sy + (cj[cells, None] - _CY[None, :]))
-        need = [pulls.ravel()]
-        lk = np.concatenate([ids[ls[s0]:ls[s0 + 1]] for s0 in cells])
-        if ibb_on and len(lk):
-            near = tb["p"][lk] < 0.5
-            x = storage(tb["link_cell"][lk])
-            n1 = storage(tb["nb1"][lk])
-            n2 = storage(tb["nb2"][lk])
-            y1 = np.where(near, n1, x)
-            y2 = np.where(near, n2, n1)
-            need += [y1, y2]
-        slots = np.unique(np.concatenate(need))
-        if 9 * len(slots) * elem_bytes > smem_cap:
-            if len(cells) > 1:  # split the group in two (cells in linear order)
-                h = len(cells) // 2
-                add_group(cells[:h])
-                add_group(cells[h:])
-            return  # a single cell over the cap stays with the per-cell kernel
-        pull_rows.append(np.searchsorted(slots, pulls))
-        if ibb_on and len(lk):
-            link_slot[lk, 0] = np.searchsorted(slots, y1)
-            link_slot[lk, 1] = np.searchsorted(slots, y2)
-        groups.append(cells)
-        slots_all.append(slots)
-        in_group[cells] = True
-
-    for o in np.unique(cell_obs[pure]):
-        add_group(np.flatnonzero(pure & (cell_obs == o)))
-    main = np.flatnonzero(~in_group)
-    order = np.concatenate([main] + groups) if groups else main
-    new_special = special[order]
-    counts = n_cell_links[order]
-    new_ls = np.zeros(n_special + 1, np.int64)
-    new_ls[1:] = np.cumsum(counts)
-    new_ids = (np.concatenate([ids[ls[s0]:ls[s0 + 1]] for s0 in order])
-               if n_links else np.zeros(0, np.int64))
-    rank = np.empty(n_special, np.int64)
-    rank[order] = np.arange(n_special)
-    gc = np.zeros(len(groups) + 1, np.int64)
-    gc[0] = len(main)
-    gc[1:] = len(main) + np.cumsum([len(g) for g in groups])
-    gs = np.zeros(len(groups) + 1, np.int64)
-    gs[1:] = np.cumsum([len(x) for x in slots_all])
-    return dict(special=new_special, link_start=new_ls, link_ids=new_ids,
-                corner_special=[int(rank[c]) for c in tb["corner_special"]],
-                corner_nb_special=[int(rank[c]) for c in tb["corner_nb_special"]],
-                n_main=len(main), group_cell_start=gc, group_slot_start=gs,
-                slot_cell=(np.concatenate(slots_all) if slots_all else np.zeros(0, np.int64)),
-                pull_slot=(np.concatenate(pull_rows) if pull_rows else np.zeros((0, 9), np.int64)),
-                link_slot=link_slot[:n_links], max_slots=max([len(x) for x in slots_all] or [0]))
-
-
 def ibb_coefficients(p):
     """[3][n] IBB coefficients of each link (lbm_problem.link_coef): the
     factors of the reference's interpolated bounce-back (nb.py:98-104),
@@ -297,8 +199,7 @@ def ibb_coefficients(p):
 class FusedEngine:
     """Device state and launch logic of a fused run (see module docstring)."""
 
-    def __init__(self, lat, obstacles, walls, corners, precision=None, drag_cap=4096,
-                 link_groups_enabled=True):
+    def __init__(self, lat, obstacles, walls, corners, precision=None, drag_cap=4096):
         self.lat = lat
         self.nx, self.ny = lat.nx, lat.ny
         self.N = self.nx * self.ny
@@ -331,16 +232,6 @@ class FusedEngine:
         nb1, nb2 = storage_index(tb["nb1"]), storage_index(tb["nb2"])
         starts = tb["obs_start"]
         corner_special, corner_nb = tb["corner_special"], tb["corner_nb_special"]
-        # Link groups: each obstacle's link cells off the walls, staged in
-        # shared memory by one block per group (lbm_problem link groups).
-        self.groups = None
-        if n_links and link_groups_enabled:
-            elem = torch.tensor([], dtype=st_dtype).element_size()
-            gr = link_groups(tb, nx, ny, self.sy, bool(lat.IBB), elem)
-            if len(gr["group_cell_start"]) > 1:
-                self.groups = gr
-                special, link_start, order = gr["special"], gr["link_start"], gr["link_ids"]
-                corner_special, corner_nb = gr["corner_special"], gr["corner_nb_special"]
 
         def i32(a):
             t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).to(dev)
@@ -362,13 +253,6 @@ class FusedEngine:
         self.t_link_p = f64(p if n_links else np.zeros(1))
         self.t_link_coef = f64(tb["coef"] if n_links else np.zeros(3))
         self.t_obs_start = i32(np.array(starts))
-        if self.groups is not None:
-            gr = self.groups
-            self.t_group_cell_start = i32(gr["group_cell_start"])
-            self.t_group_slot_start = i32(gr["group_slot_start"])
-            self.t_slot_cell = i32(gr["slot_cell"])
-            self.t_pull_slot = i32(gr["pull_slot"])
-            self.t_link_slot = i32(gr["link_slot"] if n_links else np.zeros(2))
         self.n_links = n_links
         self.n_special = n_special
 
@@ -413,16 +297,6 @@ class FusedEngine:
         P.link_p = self.t_link_p.data_ptr()
         P.link_coef = self.t_link_coef.data_ptr()
         P.special_link_ids = self.t_link_ids.data_ptr()
-        if self.groups is not None:
-            gr = self.groups
-            P.n_special_main = int(gr["n_main"])
-            P.n_link_groups = len(gr["group_cell_start"]) - 1
-            P.group_cell_start = self.t_group_cell_start.data_ptr()
-            P.group_slot_start = self.t_group_slot_start.data_ptr()
-            P.slot_cell = self.t_slot_cell.data_ptr()
-            P.pull_slot = self.t_pull_slot.data_ptr()
-            P.link_slot = self.t_link_slot.data_ptr()
-            P.group_max_slots = int(gr["max_slots"])
         P.n_obstacles = len(self.obstacles)
         P.obstacle_link_start = self.t_obs_start.data_ptr()
         P.bc_base = self.bc_base.data_ptr()

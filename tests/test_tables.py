@@ -9,7 +9,7 @@ import pytest
 
 from lbm_gb300 import _lib, geometry
 from lbm_gb300.apps import turek
-from lbm_gb300.engine import build_tables, ibb_coefficients, link_groups
+from lbm_gb300.engine import build_tables, ibb_coefficients
 
 CX = np.array([0, 1, -1, 0, 0, 1, -1, -1, 1])
 CY = np.array([0, 0, 0, 1, -1, 1, -1, 1, -1])
@@ -116,52 +116,3 @@ def test_links_leaving_the_lattice_are_refused():
     ob = types.SimpleNamespace(name="bad", boundary=np.array([[12, 3, 1]]), ibb=np.array([0.3]))
     with pytest.raises(IndexError):
         build_tables(10, 8, [ob], True)
-
-
-@pytest.mark.parametrize("case", list(_cases()), ids=lambda c: c[0])
-@pytest.mark.parametrize("pitch", [0, 8])
-def test_link_group_tables(case, pitch):
-    """Link groups (engine.link_groups): the reordered table holds every
-    special cell once, the per-cell kernel's cells first in their original
-    order; group cells are off the walls with all links to one obstacle;
-    every pull slot and IBB stencil slot names the storage cell it stands
-    for; the CSR lists and the corner indices follow the new order."""
-    _, nx, ny, obstacles, ibb = case
-    tb = build_tables(nx, ny, obstacles, ibb)
-    sy = ny if pitch == 0 else -(-ny // pitch) * pitch
-    gr = link_groups(tb, nx, ny, sy, ibb, 8, smem_cap=9 * 8 * 64)  # small cap: splits
-    sp = gr["special"]
-    assert np.array_equal(np.sort(sp), tb["special"])
-    nm = gr["n_main"]
-    assert np.all(np.diff(sp[:nm]) > 0)
-    gc, gs, slot_cell = gr["group_cell_start"], gr["group_slot_start"], gr["slot_cell"]
-    assert gc[0] == nm and gc[-1] == len(sp)
-    if case[0] != "wall_squares":
-        assert len(gc) > 2  # several groups (the small cap splits them)
-    assert np.all(np.diff(gs) * 9 * 8 <= 9 * 8 * 64)
-    obs_of = np.searchsorted(tb["obs_start"], np.arange(tb["n_links"]), side="right") - 1
-    ls, ids = gr["link_start"], gr["link_ids"]
-    for s in range(len(sp)):
-        k = ids[ls[s]:ls[s + 1]]
-        assert np.all(tb["link_cell"][k] == sp[s]) and np.all(np.diff(k) > 0)
-    for g in range(len(gc) - 1):
-        base = gs[g]
-        for s in range(gc[g], gc[g + 1]):
-            i, j = sp[s] // ny, sp[s] % ny
-            assert 1 <= i <= nx - 2 and 1 <= j <= ny - 2
-            k = ids[ls[s]:ls[s + 1]]
-            assert len(k) > 0 and len(np.unique(obs_of[k])) == 1
-            for q in range(9):
-                assert slot_cell[base + gr["pull_slot"][s - nm, q]] == (i - CX[q]) * sy + (j - CY[q])
-            if ibb:
-                for kk in k:
-                    qb = NS[tb["link_q"][kk]]
-                    st = lambda r: (r // ny) * sy + r % ny
-                    near = tb["p"][kk] < 0.5
-                    y1 = st(tb["nb1"][kk]) if near else st(tb["link_cell"][kk])
-                    y2 = st(tb["nb2"][kk]) if near else st(tb["nb1"][kk])
-                    assert slot_cell[base + gr["link_slot"][kk, 0]] == y1
-                    assert slot_cell[base + gr["link_slot"][kk, 1]] == y2
-    for c in range(4):
-        assert sp[gr["corner_special"][c]] == tb["special"][tb["corner_special"][c]]
-        assert sp[gr["corner_nb_special"][c]] == tb["special"][tb["corner_nb_special"][c]]
