@@ -32,6 +32,11 @@ __global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
   if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
+// Bytes per access of the vectorised bulk kernel of a single lattice (8 or
+// 16; rows are padded to 16 bytes, so either divides the row pitch).
+#ifndef LBM_VEC_BYTES
+#define LBM_VEC_BYTES 16
+#endif
 // Resident 128-thread blocks per SM the vectorised bulk kernel is compiled for.
 #ifndef LBM_VEC_MIN_BLOCKS
 #define LBM_VEC_MIN_BLOCKS 1
@@ -88,8 +93,9 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   const bool with_drag = MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0;
   const int tb = 256;
   const long long nb = (a.Ns + tb - 1) / tb;
-  // 16-byte vectors for the reduced storage forms (8 FP16/BF16 or 4 FP32 cells).
-  constexpr int kVec = 16 / (int)sizeof(typename St::S);
+  // LBM_VEC_BYTES-byte vectors for the reduced storage forms (16: 8 FP16/BF16
+  // or 4 FP32 cells per thread).
+  constexpr int kVec = LBM_VEC_BYTES / (int)sizeof(typename St::S);
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
   a.advance_at = with_drag ? 2 : (with_special ? 1 : 0);
   if (ev) cudaEventRecord(ev[0], st);
