@@ -32,11 +32,6 @@ __global__ void __launch_bounds__(256) k_bulk(FusedArgs a) {
   if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
-// Bytes per access of the vectorised bulk kernel of a single lattice (8 or
-// 16; rows are padded to 16 bytes, so either divides the row pitch).
-#ifndef LBM_VEC_BYTES
-#define LBM_VEC_BYTES 16
-#endif
 // Resident 128-thread blocks per SM the vectorised bulk kernel is compiled for.
 #ifndef LBM_VEC_MIN_BLOCKS
 #define LBM_VEC_MIN_BLOCKS 1
@@ -93,10 +88,12 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   const bool with_drag = MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0;
   const int tb = 256;
   const long long nb = (a.Ns + tb - 1) / tb;
-  // LBM_VEC_BYTES-byte vectors for the reduced storage forms (16: 8 FP16/BF16
-  // or 4 FP32 cells per thread).
-  constexpr int kVec = LBM_VEC_BYTES / (int)sizeof(typename St::S);
-  constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && kVec >= 4;
+  // 16-byte vectors (8 cells per thread) for the 16-bit storage forms; FP32
+  // takes the one-cell-per-thread kernel, measured faster on 8192x2048
+  // (176 vs 190 us per bulk launch with 4-cell vectors), while 8-cell
+  // vectors beat 4-cell ones for the 16-bit forms (103-112 vs 108-118 us).
+  constexpr int kVec = 16 / (int)sizeof(typename St::S);
+  constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && sizeof(typename St::S) == 2;
   a.advance_at = with_drag ? 2 : (with_special ? 1 : 0);
   if (ev) cudaEventRecord(ev[0], st);
   if (St::kFixed && MODE == LBM_MODE_STEP) {

@@ -22,8 +22,9 @@ diverged depending on how the FP32 arithmetic before the rounding was
 fused (one cell at a time: ran with mean Cd 1.8e-2 off FP64; two cells per
 packed instruction, the same operations per cell with w+ P +- M in one
 fused multiply-add: diverged within the 6,000 iterations).  At tau = 0.548 (the
-1100x200 channel of the benchmark's error study) both run.  The lattices have ny % 8 == 0, so the vectorised bulk
-kernel (16-byte loads, warp-shuffle halos) is the one tested.
+1100x200 channel of the benchmark's error study) both run.  The lattices have ny % 8 == 0, so for the 16-bit forms the
+vectorised bulk kernel (16-byte loads, warp-shuffle halos) is the one
+tested; FP32 runs the one-cell-per-thread kernel.
 """
 import numpy as np
 import pytest
