@@ -226,7 +226,7 @@ def measure_form(ny, precision, steps, warmup, tmp, peak_gbs, dist=None):
     # Per-kernel times over K more steps (events around each kernel).
     prof = (ctypes.c_double * 4)()
     _lib.call("lbm_profile_steps", ctypes.byref(eng.P), it, steps, eng.cur,
-              _lib.FLAG_CHECK_FINITE, prof, ctypes.c_void_p(stream.cuda_stream))
+              _lib.FLAG_CHECK_FINITE | eng.step_flags, prof, ctypes.c_void_p(stream.cuda_stream))
     eng.cur ^= (steps & 1)
     it += steps
     bulk_units = (lat.nx - 2) * (lat.ny - 2)

@@ -198,7 +198,8 @@ typedef struct lbm_problem {
   double* rho_out;          /* [nx*ny]   macro rho (see flags)                  */
   double* u_out;            /* [2*nx*ny] macro u                                */
   double* g_out;            /* [9*nx*ny] post-BC g (FINISH / COLLIDE_FROM_G in) */
-  uint32_t* status_flags;   /* [1] device word; bit 0 = non-finite detected     */
+  uint32_t* status_flags;   /* [1] device word; bit 0 = non-finite detected,
+                             * bit 3 = a bulk-kernel pipeline wait timed out */
 
   /* Row pitch of f[0]/f[1] in elements (0 = ny).  The distributions are
    * stored as [q][i][j] with rows of row_pitch >= ny elements; padding a
@@ -221,6 +222,10 @@ typedef struct lbm_problem {
 #define LBM_FLAG_MACRO_LAST 1u   /* write rho_out/u_out on the last step's macro */
 #define LBM_FLAG_CHECK_FINITE 2u /* set status bit 0 on NaN/Inf (cheap)          */
 #define LBM_FLAG_WALL_MACRO 4u   /* FINISH: write rho/u written by wall ops      */
+/* 16-bit forms: step with the register-pipelined bulk kernel (16-byte global
+ * loads, warp-shuffle halos) instead of the default TMA-staged one
+ * (cp.async.bulk into shared-memory stages); both give the same bits. */
+#define LBM_FLAG_BULK_REGISTERS 8u
 
 size_t lbm_problem_scratch_bytes(const lbm_problem* p);
 /* Advance n_steps iterations: each is one pass of the reference's run() loop

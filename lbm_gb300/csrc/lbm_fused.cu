@@ -19,6 +19,7 @@
 // values, and the previous macro rho/u of every special cell that corners
 // read (nb.py:254-257), in ping-pong scratch buffers.
 #include "lbm_fused.cuh"
+#include "lbm_tma.cuh"
 
 #include <math.h>
 #include <string.h>
@@ -40,6 +41,15 @@ template <class St, int V>
 __global__ void __launch_bounds__(128, LBM_VEC_MIN_BLOCKS) k_bulk_vec(FusedArgs a) {
   const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   bulk_group_vec<St, V>(a, gi);
+  if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
+}
+
+// TMA-staged bulk kernel of the 16-bit forms (lbm_tma.cuh): one lattice,
+// tiles of consecutive cells over the interior columns.
+template <class St, class Sh>
+__global__ void __launch_bounds__(Sh::kThreads, 1) k_bulk_tma(FusedArgs a, int n_tiles) {
+  const LatticeTiles<Sh> src{a, a.sy, (long long)(a.nx - 1) * a.sy};
+  bulk_tma_body<St, Sh>(src, n_tiles, a.status);
   if (a.advance_at == 0) advance_counter(a.it_dev, a.step_done);
 }
 
@@ -79,8 +89,12 @@ __global__ void k_set_it(long long* it_dev, unsigned* done, long long value) {
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-// ev (optional): four events recorded before k_bulk, k_special, k_drag and
-// after the step, for per-kernel timing.
+template <class St, class Sh>
+static int tma_blocks_per_sm() {
+  static int per_sm[64] = {};
+  return tma_prepare((const void*)k_bulk_tma<St, Sh>, Sh::kThreads, Sh::kSmem, per_sm);
+}
+
 template <class St, int MODE>
 static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   FusedArgs a = a0;
@@ -99,11 +113,24 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   if (St::kFixed && MODE == LBM_MODE_STEP) {
     const int jb = (a.ny + 255) / 256;
     k_bulk_q60<<<(unsigned)((long long)a.nx * jb), 256, 0, st>>>(a, jb);
-  } else if (kUseVec && a.sy % kVec == 0) {
-    const long long groups = (long long)a.nx * (a.sy / kVec);
-    k_bulk_vec<St, kVec><<<(unsigned)((groups + 127) / 128), 128, 0, st>>>(a);
   } else {
-    k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
+    bool launched = false;
+    if constexpr (kUseVec) {
+      if (a.sy % kVec == 0 && a.bulk_tma && a.nx > 2) {
+        using Sh = typename TmaShapeOf<St>::type;
+        const long long cells = (long long)(a.nx - 2) * a.sy;
+        const int n_tiles = (int)((cells + Sh::kCells - 1) / Sh::kCells);
+        const int slots = tma_blocks_per_sm<St, Sh>() * device_sm_count();
+        k_bulk_tma<St, Sh><<<n_tiles < slots ? n_tiles : slots, Sh::kThreads, Sh::kSmem, st>>>(
+            a, n_tiles);
+        launched = true;
+      } else if (a.sy % kVec == 0) {
+        const long long groups = (long long)a.nx * (a.sy / kVec);
+        k_bulk_vec<St, kVec><<<(unsigned)((groups + 127) / 128), 128, 0, st>>>(a);
+        launched = true;
+      }
+    }
+    if (!launched) k_bulk<St, MODE><<<(unsigned)nb, tb, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[1], st);
   if (with_special) {
@@ -215,6 +242,7 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.mode = mode;
   a.advance_at = 0;
   a.check_finite = (flags & LBM_FLAG_CHECK_FINITE) && p->status_flags ? 1 : 0;
+  a.bulk_tma = (flags & LBM_FLAG_BULK_REGISTERS) ? 0 : 1;
   a.wall_macro = (flags & LBM_FLAG_WALL_MACRO) && p->rho_out && p->u_out ? 1 : 0;
   return a;
 }
@@ -247,6 +275,16 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
     return LBM_ERR_CUDA;
   }
   return LBM_OK;
+}
+
+int tma_tile_cells(int precision) {
+  switch (precision) {
+    case LBM_PREC_F16S: return TmaShapeOf<StoreF16>::type::kCells;
+    case LBM_PREC_F16SR: return TmaShapeOf<StoreF16SR>::type::kCells;
+    case LBM_PREC_BF16S: return TmaShapeOf<StoreBF16>::type::kCells;
+    case LBM_PREC_BF16SR: return TmaShapeOf<StoreBF16SR>::type::kCells;
+    default: return 0;
+  }
 }
 
 int fused_set_it(const lbm_problem* p, long long value, cudaStream_t st) {

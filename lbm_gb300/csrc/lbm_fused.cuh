@@ -65,6 +65,7 @@ struct FusedArgs {
   double* u_out;
   double* g_out;
   unsigned* status;
+  int bulk_tma;  // 16-bit forms: TMA-staged bulk kernel (else register-pipelined)
   int mode;
   int write_macro;
   int wall_macro;
@@ -240,6 +241,11 @@ struct alignas(sizeof(S) * V) Pack {
   S v[V];
 };
 
+template <class St, int V>
+__device__ __forceinline__ void bulk_group_vec_update(const FusedArgs& a, int i, int j0,
+                                                      const Pack<typename St::S, V> (&in)[9],
+                                                      const typename St::T (&halo)[9]);
+
 // gi: group index within the lattice; every lane of the warp must call this
 // (the halo shuffles use the full mask), lanes past the last group included.
 template <class St, int V>
@@ -247,8 +253,8 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
   using S = typename St::S;
   using T = typename St::T;
   using P = Pack<S, V>;
-  const long long N = a.N, Ns = a.Ns;
-  const int ny = a.ny, sy = a.sy;
+  const long long Ns = a.Ns;
+  const int sy = a.sy;
   const int G = sy / V;
   const bool valid = gi >= 0 && gi < (long long)a.nx * G;
   const int i = valid ? (int)(gi / G) : 0;
@@ -256,7 +262,6 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
   const bool active = valid && i > 0 && i < a.nx - 1;
   const unsigned lane = threadIdx.x & 31u;
   const S* fin = (const S*)a.fin;
-  const Coef<T>& k = coef<T>(a);
 
   P in[9];
   T halo[9];  // the cell just outside the group for planes with c_y != 0
@@ -284,6 +289,24 @@ __device__ __forceinline__ void bulk_group_vec(const FusedArgs& a, long long gi)
     }
   }
   if (!active) return;
+  bulk_group_vec_update<St, V>(a, i, j0, in, halo);
+}
+
+// The update of one vector group (cells j0 .. j0+V-1 of column i) from its
+// nine source vectors and halo cells (planes with c_y = +1: in[q].v[e] is the
+// source of cell j0+e+1 and halo[q] that of j0; c_y = -1: in[q].v[e] feeds
+// j0+e-1 and halo[q] feeds j0+V-1; c_y = 0: in[q].v[e] feeds j0+e).  Shared
+// by the register-pipelined and the TMA-staged bulk kernels.
+template <class St, int V>
+__device__ __forceinline__ void bulk_group_vec_update(const FusedArgs& a, int i, int j0,
+                                                      const Pack<typename St::S, V> (&in)[9],
+                                                      const typename St::T (&halo)[9]) {
+  using S = typename St::S;
+  using T = typename St::T;
+  using P = Pack<S, V>;
+  const long long N = a.N, Ns = a.Ns;
+  const int ny = a.ny, sy = a.sy;
+  const Coef<T>& k = coef<T>(a);
 
   P out[9];
   // Cells are updated two at a time so that each plane's pair of results is

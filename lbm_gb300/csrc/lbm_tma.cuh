@@ -1,0 +1,286 @@
+// TMA-staged bulk update of the 16-bit storage forms, shared by the
+// single-lattice kernel (lbm_fused.cu) and the batched one (lbm_batch.cu).
+//
+// A persistent kernel: block b takes tiles b, b + gridDim.x, ... of at most
+// Sh::kCells consecutive storage cells of one lattice's interior columns
+// (1 .. nx-2).  For a tile of len cells starting at cell c0, the pull sources
+// of plane q are the cells c0 - c_x sy - c_y + [0, len): one producer thread
+// copies the range c0 - c_x sy + [-8, len + 8) of each plane (one 16-byte
+// vector of halo on either side, clipped to the plane) from HBM into a
+// shared-memory stage with cp.async.bulk, which completes on the stage's
+// `full` mbarrier.  The stages rotate, so several tiles' loads are in flight
+// while the consumer warps work: each consumer thread reads its group's nine
+// vectors and six halo cells from the stage, arrives on the stage's `empty`
+// mbarrier, and runs bulk_group_vec_update (the update of the
+// register-pipelined kernel, so both give the same bits).  Every wait is
+// bounded (kWaitNs): a wait that runs out sets status bit 3 and the thread
+// leaves its loop; the producer then waits (bounded) for its copies still in
+// flight before the block exits.
+//
+// Alignment: lattice rows are padded to a multiple of 8 elements (16 bytes),
+// so c0, len, sy and the plane size are multiples of 8 elements; every copy
+// starts and ends on a 16-byte boundary of the plane (the planes start on
+// 256-byte boundaries) and of its stage row (rows of kRow elements, kRow a
+// multiple of 8, at offset 0 or 8).
+#pragma once
+
+#include "lbm_fused.cuh"
+
+namespace lbm {
+
+constexpr int kTmaHalo = 8;        // one 16-byte vector of 16-bit elements
+constexpr int kTmaBarBytes = 128;  // the stages' mbarriers
+constexpr unsigned long long kWaitNs = 500ull * 1000 * 1000;
+
+// Shape of the kernel: W consumer warps of V cells per thread (tiles of
+// W * 32 * V cells), NST stages, plus one producer warp.
+template <int W, int V, int NST>
+struct TmaShape {
+  static constexpr int kWarps = W, kV = V, kStages = NST;
+  static constexpr int kConsumers = W * 32;
+  static constexpr int kThreads = kConsumers + 32;
+  static constexpr int kCells = kConsumers * V;
+  static constexpr int kRow = kCells + 2 * kTmaHalo;  // elements per plane and stage
+  static constexpr size_t kSmem = kTmaBarBytes + (size_t)NST * 9 * kRow * 2;
+  static_assert(16 * NST <= kTmaBarBytes, "two mbarriers per stage");
+  static_assert(kSmem <= 227 * 1024, "stages exceed the shared memory of a block");
+  static_assert(V == 4 || V == 8, "8- or 16-byte vectors");
+};
+// Per form, the fastest shape measured on 8192x2048 (bulk kernel, us per
+// launch; the register-pipelined kernel in brackets): FP16 8 warps x 8 cells,
+// 4 stages of 37 KB: 95.9 (104.4); BF16 12 x 4, 6 stages of 28 KB: 97.7
+// (104.3); FP16 and BF16 with stochastic rounding 16 x 4, 4 stages of
+// 37 KB: 97.0 (109.2) and 96.9 (111.0).  One block per SM in each case.
+#if defined(LBM_TMA_WARPS)  // one shape for every form (tuning builds)
+template <class St>
+struct TmaShapeOf {
+  using type = TmaShape<LBM_TMA_WARPS, LBM_TMA_V, LBM_TMA_STAGES>;
+};
+#else
+template <class St>
+struct TmaShapeOf {
+  using type = TmaShape<16, 4, 4>;
+};
+template <>
+struct TmaShapeOf<StoreF16> {
+  using type = TmaShape<8, 8, 4>;
+};
+template <>
+struct TmaShapeOf<StoreBF16> {
+  using type = TmaShape<12, 4, 6>;
+};
+#endif
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the phase of the given parity to complete; false after kWaitNs.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  do {
+    if (mbar_try_wait(bar, parity)) return true;
+  } while (global_ns() - t0 < kWaitNs);
+  return false;
+}
+// HBM -> shared memory bulk copy (16-byte aligned addresses, size a multiple
+// of 16), completing `bytes` of transaction count on bar.
+__device__ __forceinline__ void bulk_load(unsigned dst, const void* src, unsigned bytes,
+                                          unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// Source range of plane q for the tile at c0 (len cells), clipped to the
+// plane: [lo, hi) in plane elements, and where lo lands in the stage row.
+struct TmaRange {
+  long long lo, hi;
+  int dst;
+};
+__device__ __forceinline__ TmaRange tma_range(int q, long long c0, long long len, int sy,
+                                              long long Ns) {
+  const long long s0 = c0 - (long long)cx(q) * sy - kTmaHalo;
+  TmaRange r;
+  r.lo = s0 < 0 ? 0 : s0;
+  const long long h = s0 + len + 2 * kTmaHalo;
+  r.hi = h > Ns ? Ns : h;
+  r.dst = (int)(r.lo - s0);
+  return r;
+}
+
+// Tiles of one lattice: kCells consecutive cells from column 1's first cell.
+template <class Sh>
+struct LatticeTiles {
+  const FusedArgs& a;
+  long long c_begin, c_end;
+  __device__ __forceinline__ const FusedArgs& args(int) const { return a; }
+  __device__ __forceinline__ long long first(int t) const {
+    return c_begin + (long long)t * Sh::kCells;
+  }
+  __device__ __forceinline__ int count(int t) const {
+    const long long left = c_end - first(t);
+    return left < Sh::kCells ? (int)left : Sh::kCells;
+  }
+};
+
+// Tiles of a batch: (lattice, first cell, cells, -) records.
+struct BatchTiles {
+  const FusedArgs* a;
+  const int4* tiles;
+  __device__ __forceinline__ const FusedArgs& args(int t) const { return a[tiles[t].x]; }
+  __device__ __forceinline__ long long first(int t) const { return tiles[t].y; }
+  __device__ __forceinline__ int count(int t) const { return tiles[t].z; }
+};
+
+// The kernel body; every thread of the block calls it.  status: where a
+// timed-out wait is reported.
+template <class St, class Sh, class Src>
+__device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsigned* status) {
+  using S = typename St::S;
+  using T = typename St::T;
+  constexpr int V = Sh::kV, NST = Sh::kStages, kConsumers = Sh::kConsumers, kRow = Sh::kRow;
+  using P = Pack<S, V>;
+  static_assert(sizeof(S) == 2, "16-bit storage forms only");
+  extern __shared__ __align__(128) unsigned char smem[];
+  const unsigned full0 = smem_addr(smem), empty0 = full0 + 8 * NST;
+  S* stage = reinterpret_cast<S*>(smem + kTmaBarBytes);
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, kConsumers);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == kConsumers) {
+    // producer
+    int k = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
+      const int s = k % NST;
+      if (k >= NST && !mbar_wait(empty0 + 8 * s, ((k / NST) - 1) & 1)) {
+        ok = false;
+        break;
+      }
+      const FusedArgs& a = src.args(t);
+      const S* fin = (const S*)a.fin;
+      const long long Ns = a.Ns, c0 = src.first(t);
+      const int sy = a.sy, len = src.count(t);
+      unsigned bytes = 0;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        const TmaRange r = tma_range(q, c0, len, sy, Ns);
+        bytes += (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S);
+      }
+      mbar_expect_tx(full0 + 8 * s, bytes);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        const TmaRange r = tma_range(q, c0, len, sy, Ns);
+        bulk_load(smem_addr(stage + (size_t)(s * 9 + q) * kRow + r.dst), fin + q * Ns + r.lo,
+                  (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S), full0 + 8 * s);
+      }
+    }
+    if (!ok) {
+      if (status) atomicOr(status, 8u);
+      // the copies of the last issued tiles may still be in flight
+      for (int kk = k - NST < 0 ? 0 : k - NST; kk < k; ++kk)
+        mbar_wait(full0 + 8 * (kk % NST), (kk / NST) & 1);
+    }
+  } else if (tid < kConsumers) {
+    int k = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
+      const int s = k % NST;
+      if (!mbar_wait(full0 + 8 * s, (k / NST) & 1)) {
+        if (status) atomicOr(status, 8u);
+        break;
+      }
+      const FusedArgs& a = src.args(t);
+      const int sy = a.sy;
+      const int off = tid * V;
+      const long long c = src.first(t) + off;
+      const bool act = off < src.count(t);
+      const int i = (int)(c / sy);
+      const int j0 = (int)(c - (long long)i * sy);
+      P in[9];
+      T halo[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        const S* row = stage + (size_t)(s * 9 + q) * kRow + kTmaHalo + off;
+        if (act) in[q] = *reinterpret_cast<const P*>(row);
+        if (cy(q) == 1)  // cell j0 pulls from j0 - 1 (zero at a column start)
+          halo[q] = act && j0 > 0 ? St::load(row - 1) : T(0);
+        else if (cy(q) == -1)  // cell j0 + V - 1 pulls from j0 + V (zero past the column)
+          halo[q] = act && j0 + V < sy ? St::load(row + V) : T(0);
+        else
+          halo[q] = T(0);
+      }
+      mbar_arrive(empty0 + 8 * s);
+      if (act) bulk_group_vec_update<St, V>(a, i, j0, in, halo);
+    }
+  }
+}
+
+// Host: SMs of the current device (cached per device).
+inline int device_sm_count() {
+  static int count[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!count[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    count[dev] = n > 0 ? n : 1;
+  }
+  return count[dev];
+}
+
+// Host: opts a TMA-staged kernel into its dynamic shared memory and returns
+// how many of its blocks fit on one SM (once per device; cache[64] per
+// kernel).
+inline int tma_prepare(const void* kernel, int threads, size_t smem, int* cache) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!cache[dev]) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem);
+    cache[dev] = n > 0 ? n : 1;
+  }
+  return cache[dev];
+}
+
+// Cells per tile of the form's TMA-staged kernel (0: the form has none).
+int tma_tile_cells(int precision);
+
+}  // namespace lbm

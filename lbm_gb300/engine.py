@@ -267,6 +267,9 @@ class FusedEngine:
         n_obs = max(1, len(self.obstacles))
         self.drag_hist = torch.zeros((self.drag_cap, n_obs, 2), dtype=torch.float64, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        # 16-bit forms step through the TMA-staged bulk kernel unless
+        # bulk_kernel is set to "registers" (lbm_advance flags)
+        self.bulk_kernel = "tma"
 
         # ---- problem descriptor
         P = _lib.Problem()
@@ -334,6 +337,12 @@ class FusedEngine:
         self.P.bc_scale_len = int(self.bc_scale.numel())
 
     # -------------------------------------------------------------- stepping
+    @property
+    def step_flags(self):
+        if self.bulk_kernel not in ("tma", "registers"):
+            raise ValueError("bulk_kernel is 'tma' or 'registers'")
+        return _lib.FLAG_BULK_REGISTERS if self.bulk_kernel == "registers" else 0
+
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -353,6 +362,7 @@ class FusedEngine:
         if n <= 0:
             return
         flags = (_lib.FLAG_MACRO_LAST if macro_last else 0) | _lib.FLAG_CHECK_FINITE
+        flags |= self.step_flags
         if macro_last:
             self.lat.device_field("rho", True)
             self.lat.device_field("u", True)
@@ -419,6 +429,8 @@ class FusedEngine:
         if s & 4:
             raise RuntimeError("batched step: special-cell tiles stopped waiting for "
                                "their lattice's bulk tiles")
+        if s & 8:
+            raise RuntimeError("bulk kernel: a shared-memory stage wait timed out")
 
     # --------------------------------------------------------- snapshot/restore
     def snapshot(self):
