@@ -70,6 +70,7 @@ extern "C" {
 #define LBM_MODE_STEP 1            /* stream+BC of f_in, then macro+eq+collide      */
 #define LBM_MODE_FINISH 2          /* stream+BC of f_in into g_out, no collision    */
 
+/* 2 (lbm_batch_config.bulk_tma added). */
 int lbm_abi_version(void);
 const char* lbm_last_error_string(void);
 /* Number of SMs and name of the current device (for logs/tuning). */
@@ -285,6 +286,10 @@ typedef struct lbm_batch_config {
                                     kernel (cells per thread = this / element)    */
   int32_t tile_rounds;           /* 1..64: a vector bulk tile is this many block-
                                     widths of groups (a thread loops over them)   */
+  int32_t bulk_tma;              /* 1 (16-bit forms only): the bulk phase runs the
+                                    TMA-staged persistent kernel, on tiles of its
+                                    own size; bulk_threads, bulk_blocks_per_sm,
+                                    vec_bytes and tile_rounds then do not apply */
 } lbm_batch_config;
 int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32_t n_cases,
                      const lbm_batch_config* cfg);

@@ -75,7 +75,8 @@ class BatchConfig(ctypes.Structure):
 
     _fields_ = [("bulk_threads", _i32), ("bulk_blocks_per_sm", _i32),
                 ("special_blocks_per_sm", _i32), ("scalar_tile_cells", _i32),
-                ("persistent", _i32), ("vec_bytes", _i32), ("tile_rounds", _i32)]
+                ("persistent", _i32), ("vec_bytes", _i32), ("tile_rounds", _i32),
+                ("bulk_tma", _i32)]
 
 
 class Adjoint(ctypes.Structure):

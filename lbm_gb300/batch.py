@@ -155,7 +155,7 @@ class Batch:
         c = _lib.BatchConfig(cfg["bulk_threads"], cfg["bulk_blocks_per_sm"],
                              cfg["special_blocks_per_sm"], cfg["scalar_tile_cells"],
                              int(cfg.get("persistent", 1)), int(cfg.get("vec_bytes", 16)),
-                             int(cfg.get("tile_rounds", 1)))
+                             int(cfg.get("tile_rounds", 1)), int(cfg.get("bulk_tma", 0)))
         h = ctypes.c_void_p()
         _lib.call("lbm_batch_create", ctypes.byref(h), arr, len(self.engines), ctypes.byref(c))
         self.handle = h
@@ -193,10 +193,14 @@ class Batch:
             self.handle = None
 
 
+# storage forms with a TMA-staged bulk kernel (lbm_batch_config.bulk_tma)
+TMA_FORMS = ("f16s", "f16sr", "bf16s", "bf16sr")
+
+
 def default_config():
     return {"bulk_threads": 128, "bulk_blocks_per_sm": 8, "special_blocks_per_sm": 8,
             "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 0, "vec_bytes": 8,
-            "tile_rounds": 4}
+            "tile_rounds": 4, "bulk_tma": 0}
 
 
 def time_batch(batch, n_steps, k=None):
@@ -221,13 +225,18 @@ def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200), verbos
     iteration count for every K).  Returns (best config, table of trials).
     """
     # one block per tile (the persistent grid size does not apply), then
-    # persistent blocks; a dict of value lists or a list of such dicts
-    space = space or [
-        {"persistent": [0], "tile_rounds": [2, 4, 8], "vec_bytes": [16, 8],
-         "bulk_threads": [64, 128], "k_steps": [50]},
-        {"persistent": [1], "tile_rounds": [4, 8], "vec_bytes": [16, 8],
-         "bulk_threads": [128], "bulk_blocks_per_sm": [8, 12], "k_steps": [50]},
-    ]
+    # persistent blocks, then (16-bit forms) the TMA-staged bulk kernel with
+    # either schedule of the special cells; a dict of value lists or a list
+    # of such dicts
+    if space is None:
+        space = [
+            {"persistent": [0], "tile_rounds": [2, 4, 8], "vec_bytes": [16, 8],
+             "bulk_threads": [64, 128], "k_steps": [50]},
+            {"persistent": [1], "tile_rounds": [4, 8], "vec_bytes": [16, 8],
+             "bulk_threads": [128], "bulk_blocks_per_sm": [8, 12], "k_steps": [50]},
+        ]
+        if batch.precision in TMA_FORMS:
+            space.append({"bulk_tma": [1], "persistent": [0, 1], "k_steps": [50]})
     spaces = [space] if isinstance(space, dict) else list(space)
     candidates = []
     for sp in spaces:

@@ -113,7 +113,7 @@ const size_t kMaxGraphs = 16;
 
 using namespace lbm;
 
-extern "C" int lbm_abi_version(void) { return 1; }
+extern "C" int lbm_abi_version(void) { return 2; }
 
 extern "C" const char* lbm_last_error_string(void) { return g_err; }
 

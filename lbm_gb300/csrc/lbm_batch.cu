@@ -4,7 +4,9 @@
 // whose blocks pull tiles from an atomic work queue:
 //
 //   k_batch_bulk     tiles of bulk cells of every lattice (16-byte vector
-//                    groups where ny % V == 0, single cells otherwise)
+//                    groups where ny % V == 0, single cells otherwise), or
+//                    k_batch_bulk_tma: the TMA-staged persistent kernel of
+//                    the 16-bit forms (lbm_tma.cuh) over every lattice's tiles
 //   k_batch_special  tiles of special cells of every lattice
 //   k_batch_drag     one block per (lattice, obstacle)
 //
@@ -19,6 +21,7 @@
 #include <vector>
 
 #include "lbm_fused.cuh"
+#include "lbm_tma.cuh"
 
 struct lbm_batch {
   int n_cases;
@@ -26,7 +29,7 @@ struct lbm_batch {
   lbm_batch_config cfg;
   int sm_count;
   lbm::FusedArgs* d_args;   // [2][n_cases]
-  int4* d_bulk_tiles;       // (case, first, count, vectorised)
+  int4* d_bulk_tiles;       // (case, first, count, vectorised); TMA: (case, first cell, cells, 2)
   int n_bulk_tiles;
   int4* d_special_tiles;    // (case, first, count, 0)
   int n_special_tiles;
@@ -141,6 +144,19 @@ __global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_batch_special(c
   if (last) advance_counter(it_dev, queue + 2);
 }
 
+// TMA-staged bulk phase: persistent blocks over every lattice's tiles (tiles
+// of the largest lattices first, taken round-robin by block).
+template <class St, class Sh>
+__global__ void __launch_bounds__(Sh::kThreads, 1) k_batch_bulk_tma(
+    const FusedArgs* __restrict__ args, const int4* __restrict__ tiles, int n_tiles,
+    unsigned* queue, long long* it_dev, int last) {
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    queue[1] = 0;  // the special phase of this iteration starts from tile 0
+  const BatchTiles src{args, tiles};
+  bulk_tma_body<St, Sh>(src, n_tiles, args[0].status);
+  if (last) advance_counter(it_dev, queue + 2);
+}
+
 // One block of 256 threads per (lattice, obstacle) item.
 __global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict__ args,
                                                     const int2* __restrict__ items, int n_items,
@@ -161,6 +177,30 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
   const int bulk_last = !drag && !special, special_last = !drag && special;
   for (int k = 0; k < n_steps; ++k) {
     const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
+    if constexpr (sizeof(typename St::S) == 2 && St::kShift) {
+      if (b->cfg.bulk_tma) {
+        using Sh = typename TmaShapeOf<St>::type;
+        static int per_sm[64] = {};
+        const int slots =
+            tma_prepare((const void*)k_batch_bulk_tma<St, Sh>, Sh::kThreads, Sh::kSmem, per_sm) *
+            b->sm_count;
+        k_batch_bulk_tma<St, Sh>
+            <<<b->n_bulk_tiles < slots ? b->n_bulk_tiles : slots, Sh::kThreads, Sh::kSmem, st>>>(
+                args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
+        if (special) {
+          if (b->cfg.persistent)
+            k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
+                                                    b->d_queue, b->d_it, special_last);
+          else
+            k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(
+                args, b->d_special_tiles, b->d_queue, b->d_it, special_last);
+        }
+        if (drag)
+          k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items,
+                                                        b->d_queue, b->d_it);
+        continue;
+      }
+    }
     if (b->cfg.persistent) {
       k_batch_bulk<St, VB, kVecOnly><<<gb, b->cfg.bulk_threads, 0, st>>>(
           args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
@@ -247,7 +287,7 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       cfg->scalar_tile_cells < 32 || cfg->scalar_tile_cells > (1 << 20) ||
       (cfg->persistent != 0 && cfg->persistent != 1) ||
       (cfg->vec_bytes != 8 && cfg->vec_bytes != 16) || cfg->tile_rounds < 1 ||
-      cfg->tile_rounds > 64) {
+      cfg->tile_rounds > 64 || (cfg->bulk_tma != 0 && cfg->bulk_tma != 1)) {
     set_error("lbm_batch_create: bad config (threads %d, blocks/SM %d/%d, tile %d)",
               cfg->bulk_threads, cfg->bulk_blocks_per_sm, cfg->special_blocks_per_sm,
               cfg->scalar_tile_cells);
@@ -264,6 +304,11 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
   const int V = (prec == LBM_PREC_F64 || prec == LBM_PREC_Q60)
                     ? 1
                     : cfg->vec_bytes / (prec == LBM_PREC_F32 ? 4 : 2);
+  const int tma_cells = cfg->bulk_tma ? tma_tile_cells(prec) : 0;
+  if (cfg->bulk_tma && !tma_cells) {
+    set_error("lbm_batch_create: bulk_tma needs a 16-bit storage form");
+    return LBM_ERR_ARG;
+  }
   std::vector<FusedArgs> args(2 * (size_t)n_cases);
   std::vector<int4> bulk, special;
   std::vector<int2> drag;
@@ -286,7 +331,15 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
     }
     const int sy = p.row_pitch > 0 ? p.row_pitch : p.ny;
     const long long N = (long long)p.nx * sy;  // storage cells, padding included
-    if (V > 1 && sy % V == 0) {
+    if (tma_cells) {
+      if (sy % 8) {
+        set_error("lbm_batch_create: bulk_tma needs rows padded to 16 bytes (lattice %d)", c);
+        return LBM_ERR_ARG;
+      }
+      // the interior columns 1 .. nx-2, tma_cells per tile
+      for (long long x = sy; x < N - sy; x += tma_cells)
+        bulk.push_back(make_int4(c, (int)x, (int)std::min<long long>(tma_cells, N - sy - x), 2));
+    } else if (V > 1 && sy % V == 0) {
       const long long groups = (long long)p.nx * (sy / V);
       // tile_rounds block-widths of groups per tile
       const int tg = cfg->bulk_threads * cfg->tile_rounds;

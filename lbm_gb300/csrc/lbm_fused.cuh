@@ -9,7 +9,7 @@
 
 namespace lbm {
 
-struct FusedArgs {
+struct alignas(16) FusedArgs {
   int nx, ny;
   long long N;          // nx * ny: plane size of the FP64 reference-layout arrays
   int sy;               // row pitch of the distribution storage (>= ny)

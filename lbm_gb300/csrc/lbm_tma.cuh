@@ -11,8 +11,9 @@
 // `full` mbarrier.  The stages rotate, so several tiles' loads are in flight
 // while the consumer warps work: each consumer thread reads its group's nine
 // vectors and six halo cells from the stage, arrives on the stage's `empty`
-// mbarrier, and runs bulk_group_vec_update (the update of the
-// register-pipelined kernel, so both give the same bits).  Every wait is
+// mbarrier (batched tiles: after the update, see BatchTiles), and runs
+// bulk_group_vec_update (the update of the register-pipelined kernel, so
+// both give the same bits).  Every wait is
 // bounded (kWaitNs): a wait that runs out sets status bit 3 and the thread
 // leaves its loop; the producer then waits (bounded) for its copies still in
 // flight before the block exits.
@@ -41,7 +42,9 @@ struct TmaShape {
   static constexpr int kThreads = kConsumers + 32;
   static constexpr int kCells = kConsumers * V;
   static constexpr int kRow = kCells + 2 * kTmaHalo;  // elements per plane and stage
-  static constexpr size_t kSmem = kTmaBarBytes + (size_t)NST * 9 * kRow * 2;
+  // barriers | one FusedArgs per stage (batched tiles) | stages
+  static constexpr size_t kArgsBytes = (size_t)NST * sizeof(FusedArgs);
+  static constexpr size_t kSmem = kTmaBarBytes + kArgsBytes + (size_t)NST * 9 * kRow * 2;
   static_assert(16 * NST <= kTmaBarBytes, "two mbarriers per stage");
   static_assert(kSmem <= 227 * 1024, "stages exceed the shared memory of a block");
   static_assert(V == 4 || V == 8, "8- or 16-byte vectors");
@@ -137,9 +140,13 @@ __device__ __forceinline__ TmaRange tma_range(int q, long long c0, long long len
   return r;
 }
 
+static_assert(sizeof(FusedArgs) % 16 == 0, "FusedArgs records are copied with cp.async.bulk");
+
 // Tiles of one lattice: kCells consecutive cells from column 1's first cell.
+// The lattice's FusedArgs is the kernel parameter.
 template <class Sh>
 struct LatticeTiles {
+  static constexpr bool kStageArgs = false;
   const FusedArgs& a;
   long long c_begin, c_end;
   __device__ __forceinline__ const FusedArgs& args(int) const { return a; }
@@ -152,8 +159,13 @@ struct LatticeTiles {
   }
 };
 
-// Tiles of a batch: (lattice, first cell, cells, -) records.
+// Tiles of a batch: (lattice, first cell, cells, -) records.  The producer
+// copies each tile's FusedArgs into its stage with the populations, so that
+// the consumers read it from shared memory (read from global memory, every
+// field would be loaded again after each store: the compiler cannot tell
+// the records from the distributions they point to).
 struct BatchTiles {
+  static constexpr bool kStageArgs = true;
   const FusedArgs* a;
   const int4* tiles;
   __device__ __forceinline__ const FusedArgs& args(int t) const { return a[tiles[t].x]; }
@@ -170,9 +182,11 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
   constexpr int V = Sh::kV, NST = Sh::kStages, kConsumers = Sh::kConsumers, kRow = Sh::kRow;
   using P = Pack<S, V>;
   static_assert(sizeof(S) == 2, "16-bit storage forms only");
+  constexpr bool kStageArgs = Src::kStageArgs;
   extern __shared__ __align__(128) unsigned char smem[];
   const unsigned full0 = smem_addr(smem), empty0 = full0 + 8 * NST;
-  S* stage = reinterpret_cast<S*>(smem + kTmaBarBytes);
+  FusedArgs* stage_args = reinterpret_cast<FusedArgs*>(smem + kTmaBarBytes);
+  S* stage = reinterpret_cast<S*>(smem + kTmaBarBytes + Sh::kArgsBytes);
   const int tid = threadIdx.x;
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
@@ -196,13 +210,15 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
       const S* fin = (const S*)a.fin;
       const long long Ns = a.Ns, c0 = src.first(t);
       const int sy = a.sy, len = src.count(t);
-      unsigned bytes = 0;
+      unsigned bytes = kStageArgs ? (unsigned)sizeof(FusedArgs) : 0u;
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
         const TmaRange r = tma_range(q, c0, len, sy, Ns);
         bytes += (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S);
       }
       mbar_expect_tx(full0 + 8 * s, bytes);
+      if (kStageArgs)
+        bulk_load(smem_addr(stage_args + s), &a, (unsigned)sizeof(FusedArgs), full0 + 8 * s);
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
         const TmaRange r = tma_range(q, c0, len, sy, Ns);
@@ -224,7 +240,7 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
         if (status) atomicOr(status, 8u);
         break;
       }
-      const FusedArgs& a = src.args(t);
+      const FusedArgs& a = kStageArgs ? stage_args[s] : src.args(t);
       const int sy = a.sy;
       const int off = tid * V;
       const long long c = src.first(t) + off;
@@ -244,8 +260,12 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
         else
           halo[q] = T(0);
       }
-      mbar_arrive(empty0 + 8 * s);
+      // With the FusedArgs in the stage, the stage is released after the
+      // update (its record is read until then), else as soon as the
+      // populations are in registers.
+      if (!kStageArgs) mbar_arrive(empty0 + 8 * s);
       if (act) bulk_group_vec_update<St, V>(a, i, j0, in, halo);
+      if (kStageArgs) mbar_arrive(empty0 + 8 * s);
     }
   }
 }

@@ -25,7 +25,7 @@ def test_library_builds_and_loads():
     path = _build.build()
     assert os.path.exists(path)
     L = ctypes.CDLL(path)
-    assert L.lbm_abi_version() == 1
+    assert L.lbm_abi_version() == 2
 
 
 def test_every_declared_symbol_is_exported():

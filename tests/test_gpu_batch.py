@@ -38,14 +38,18 @@ def _finish(batch, steps):
 
 
 # persistent: 1 work-queue kernels, 0 one block per tile; rounds: block-widths
-# of vector groups per bulk tile.
-@pytest.mark.parametrize("precision,persistent,vec_bytes,rounds", [
-    ("f16s", 1, 16, 1), ("f64", 1, 16, 1), ("f16sr", 0, 8, 1), ("f16sr", 1, 8, 4),
-    ("f16sr", 0, 16, 3), ("q60", 0, 16, 1)])
-def test_batch_equals_single_lattices(cuda, precision, persistent, vec_bytes, rounds):
+# of vector groups per bulk tile; tma: the TMA-staged bulk kernel (16-bit
+# forms; the single lattices step through it too, so this also compares the
+# two bulk kernels where tma is 0).
+@pytest.mark.parametrize("precision,persistent,vec_bytes,rounds,tma", [
+    ("f16s", 1, 16, 1, 0), ("f64", 1, 16, 1, 0), ("f16sr", 0, 8, 1, 0), ("f16sr", 1, 8, 4, 0),
+    ("f16sr", 0, 16, 3, 0), ("q60", 0, 16, 1, 0), ("f16s", 1, 16, 1, 1), ("f16sr", 0, 16, 1, 1),
+    ("bf16s", 0, 16, 1, 1), ("bf16sr", 1, 16, 1, 1)])
+def test_batch_equals_single_lattices(cuda, precision, persistent, vec_bytes, rounds, tma):
     steps = 120
     cfg = default_config()
-    cfg.update(persistent=persistent, vec_bytes=vec_bytes, bulk_threads=64, tile_rounds=rounds)
+    cfg.update(persistent=persistent, vec_bytes=vec_bytes, bulk_threads=64, tile_rounds=rounds,
+               bulk_tma=tma)
     b = Batch(_apps(), precision=precision, config=cfg)
     b.advance(steps, k=40)
     b.check()
