@@ -157,24 +157,44 @@ __global__ void __launch_bounds__(Sh::kThreads, 1) k_batch_bulk_tma(
   if (last) advance_counter(it_dev, queue + 2);
 }
 
-// One block of 256 threads per (lattice, obstacle) item.
+// One block of 256 threads per (lattice, obstacle) item.  It runs on a second
+// stream after the special-cell kernel has advanced the shared counter
+// (FusedArgs.drag_it_offset 2), beside the next iteration's bulk phase.
 __global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict__ args,
-                                                    const int2* __restrict__ items, int n_items,
-                                                    unsigned* queue, long long* it_dev) {
+                                                    const int2* __restrict__ items, int n_items) {
   if ((int)blockIdx.x < n_items) {
     const int2 it = items[blockIdx.x];
     drag_obstacle(args[it.x], it.y);
   }
-  advance_counter(it_dev, queue + 2);  // the drag kernel is always last
 }
 
 template <class St, int VB, bool kVecOnly>
 void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t st) {
   const int gb = b->sm_count * b->cfg.bulk_blocks_per_sm;
   const int gs = b->sm_count * b->cfg.special_blocks_per_sm;
-  // The step's last kernel advances the shared iteration counter.
+  // The special-cell kernel (the bulk kernel without special cells)
+  // advances the shared iteration counter; the drag kernel of iteration k
+  // runs on a second stream beside the bulk phase of k + 1 and is waited for
+  // by the special phase of k + 1, which rewrites the per-link terms.
   const bool drag = b->n_drag_items > 0, special = b->n_special_tiles > 0;
-  const int bulk_last = !drag && !special, special_last = !drag && special;
+  const int bulk_last = !special, special_last = special;
+  DragLane* lane = drag && LBM_DRAG_SIDE ? drag_lane() : nullptr;
+  bool drag_pending = false;
+  auto wait_drag = [&]() {
+    if (drag_pending) cudaStreamWaitEvent(st, lane->ev_drag, 0);
+  };
+  auto launch_drag = [&](const FusedArgs* args) {
+    if (!drag) return;
+    if (lane) {
+      cudaEventRecord(lane->ev_special, st);
+      cudaStreamWaitEvent(lane->sd, lane->ev_special, 0);
+      k_batch_drag<<<b->n_drag_items, 256, 0, lane->sd>>>(args, b->d_drag_items, b->n_drag_items);
+      cudaEventRecord(lane->ev_drag, lane->sd);
+      drag_pending = true;
+    } else {
+      k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items);
+    }
+  };
   for (int k = 0; k < n_steps; ++k) {
     const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
     if constexpr (sizeof(typename St::S) == 2 && St::kShift) {
@@ -188,6 +208,7 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
             <<<b->n_bulk_tiles < slots ? b->n_bulk_tiles : slots, Sh::kThreads, Sh::kSmem, st>>>(
                 args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
         if (special) {
+          wait_drag();
           if (b->cfg.persistent)
             k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
                                                     b->d_queue, b->d_it, special_last);
@@ -195,29 +216,30 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
             k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(
                 args, b->d_special_tiles, b->d_queue, b->d_it, special_last);
         }
-        if (drag)
-          k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items,
-                                                        b->d_queue, b->d_it);
+        launch_drag(args);
         continue;
       }
     }
     if (b->cfg.persistent) {
       k_batch_bulk<St, VB, kVecOnly><<<gb, b->cfg.bulk_threads, 0, st>>>(
           args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
-      if (special)
+      if (special) {
+        wait_drag();
         k_batch_special<St><<<gs, 128, 0, st>>>(args, b->d_special_tiles, b->n_special_tiles,
                                                 b->d_queue, b->d_it, special_last);
+      }
     } else {
       k_batch_bulk_grid<St, VB, kVecOnly><<<b->n_bulk_tiles, b->cfg.bulk_threads, 0, st>>>(
           args, b->d_bulk_tiles, b->d_queue, b->d_it, bulk_last);
-      if (special)
+      if (special) {
+        wait_drag();
         k_batch_special_grid<St><<<b->n_special_tiles, 128, 0, st>>>(
             args, b->d_special_tiles, b->d_queue, b->d_it, special_last);
+      }
     }
-    if (drag)
-      k_batch_drag<<<b->n_drag_items, 256, 0, st>>>(args, b->d_drag_items, b->n_drag_items,
-                                                    b->d_queue, b->d_it);
+    launch_drag(args);
   }
+  if (drag_pending) cudaStreamWaitEvent(st, lane->ev_drag, 0);  // join
 }
 
 template <class St>
@@ -326,6 +348,7 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       a.fin = p.f[par];
       a.fout = p.f[par ^ 1];
       a.advance_at = -1;  // the batch kernels advance the shared counter
+      a.drag_it_offset = 2;  // k_batch_drag runs after the special phase advanced it
       a.write_macro = 0;
       args[(size_t)par * n_cases + c] = a;
     }

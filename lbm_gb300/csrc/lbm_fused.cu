@@ -95,11 +95,16 @@ static int tma_blocks_per_sm() {
   return tma_prepare((const void*)k_bulk_tma<St, Sh>, Sh::kThreads, Sh::kSmem, per_sm);
 }
 
+// lane (optional): the drag kernel of a step goes to lane->sd beside the next
+// step's bulk kernel; *drag_pending tells whether a drag kernel of this
+// enqueue is on lane->sd.
 template <class St, int MODE>
-static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
+static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev, DragLane* lane,
+                        bool* drag_pending) {
   FusedArgs a = a0;
   const bool with_special = a.n_special > 0;
   const bool with_drag = MODE != LBM_MODE_COLLIDE_FROM_G && a.drag_hist && a.n_obs > 0 && a.n_links > 0;
+  const bool side = lane && with_drag && with_special && MODE == LBM_MODE_STEP && !ev;
   const int tb = 256;
   const long long nb = (a.Ns + tb - 1) / tb;
   // 16-byte vectors (8 cells per thread) for the 16-bit storage forms; FP32
@@ -108,7 +113,8 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   // vectors beat 4-cell ones for the 16-bit forms (103-112 vs 108-118 us).
   constexpr int kVec = 16 / (int)sizeof(typename St::S);
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && sizeof(typename St::S) == 2;
-  a.advance_at = with_drag ? 2 : (with_special ? 1 : 0);
+  a.advance_at = with_drag && !side ? 2 : (with_special ? 1 : 0);
+  a.drag_it_offset = side ? 2 : 1;
   if (ev) cudaEventRecord(ev[0], st);
   if (St::kFixed && MODE == LBM_MODE_STEP) {
     const int jb = (a.ny + 255) / 256;
@@ -135,19 +141,32 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev) {
   if (ev) cudaEventRecord(ev[1], st);
   if (with_special) {
     const int ts = 128;
+    // the previous step's drag kernel reads the per-link terms written here
+    if (side && *drag_pending) cudaStreamWaitEvent(st, lane->ev_drag, 0);
     k_special<St, MODE><<<(a.n_special + ts - 1) / ts, ts, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[2], st);
-  if (with_drag) k_drag<<<a.n_obs, 256, 0, st>>>(a);
+  if (with_drag && side) {
+    cudaEventRecord(lane->ev_special, st);
+    cudaStreamWaitEvent(lane->sd, lane->ev_special, 0);
+    k_drag<<<a.n_obs, 256, 0, lane->sd>>>(a);
+    cudaEventRecord(lane->ev_drag, lane->sd);
+    *drag_pending = true;
+  } else if (with_drag) {
+    k_drag<<<a.n_obs, 256, 0, st>>>(a);
+  }
   if (ev) cudaEventRecord(ev[3], st);
 }
 
 template <class St>
-static void launch_store(const FusedArgs& a, int mode, cudaStream_t st, cudaEvent_t* ev) {
+static void launch_store(const FusedArgs& a, int mode, cudaStream_t st, cudaEvent_t* ev,
+                         DragLane* lane, bool* drag_pending) {
   switch (mode) {
-    case LBM_MODE_COLLIDE_FROM_G: launch_mode<St, LBM_MODE_COLLIDE_FROM_G>(a, st, ev); break;
-    case LBM_MODE_STEP: launch_mode<St, LBM_MODE_STEP>(a, st, ev); break;
-    default: launch_mode<St, LBM_MODE_FINISH>(a, st, ev); break;
+    case LBM_MODE_COLLIDE_FROM_G:
+      launch_mode<St, LBM_MODE_COLLIDE_FROM_G>(a, st, ev, lane, drag_pending);
+      break;
+    case LBM_MODE_STEP: launch_mode<St, LBM_MODE_STEP>(a, st, ev, lane, drag_pending); break;
+    default: launch_mode<St, LBM_MODE_FINISH>(a, st, ev, lane, drag_pending); break;
   }
 }
 
@@ -233,6 +252,7 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.link_force = sc + 24 * ns;
   a.drag_hist = p->drag_hist;
   a.drag_cap = p->drag_cap > 0 ? p->drag_cap : 1;
+  a.drag_it_offset = 1;
   a.n_obs = p->n_obstacles;
   a.obs_start = p->obstacle_link_start;
   a.rho_out = p->rho_out;
@@ -253,6 +273,9 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
                   unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev) {
   FusedArgs a = make_args(p, mode, flags);
   if (set_it) k_set_it<<<1, 1, 0, st>>>(a.it_dev, a.step_done, it0);
+  // per-kernel timing (ev) keeps every kernel on st
+  DragLane* lane = ev || !LBM_DRAG_SIDE ? nullptr : drag_lane();
+  bool drag_pending = false;
   for (int k = 0; k < n_steps; ++k) {
     const int par = (parity + k) & 1;  // f[par] holds g_up of the previous iteration
     a.fin = p->f[par];
@@ -260,15 +283,16 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
     a.write_macro = (flags & LBM_FLAG_MACRO_LAST) && k == n_steps - 1 && p->rho_out && p->u_out;
     cudaEvent_t* e = ev ? ev + 4 * k : nullptr;
     switch (p->precision) {
-      case LBM_PREC_F64: launch_store<StoreF64>(a, mode, st, e); break;
-      case LBM_PREC_F32: launch_store<StoreF32>(a, mode, st, e); break;
-      case LBM_PREC_F16S: launch_store<StoreF16>(a, mode, st, e); break;
-      case LBM_PREC_Q60: launch_store<StoreQ60>(a, mode, st, e); break;
-      case LBM_PREC_F16SR: launch_store<StoreF16SR>(a, mode, st, e); break;
-      case LBM_PREC_BF16SR: launch_store<StoreBF16SR>(a, mode, st, e); break;
-      default: launch_store<StoreBF16>(a, mode, st, e); break;
+      case LBM_PREC_F64: launch_store<StoreF64>(a, mode, st, e, lane, &drag_pending); break;
+      case LBM_PREC_F32: launch_store<StoreF32>(a, mode, st, e, lane, &drag_pending); break;
+      case LBM_PREC_F16S: launch_store<StoreF16>(a, mode, st, e, lane, &drag_pending); break;
+      case LBM_PREC_Q60: launch_store<StoreQ60>(a, mode, st, e, lane, &drag_pending); break;
+      case LBM_PREC_F16SR: launch_store<StoreF16SR>(a, mode, st, e, lane, &drag_pending); break;
+      case LBM_PREC_BF16SR: launch_store<StoreBF16SR>(a, mode, st, e, lane, &drag_pending); break;
+      default: launch_store<StoreBF16>(a, mode, st, e, lane, &drag_pending); break;
     }
   }
+  if (drag_pending) cudaStreamWaitEvent(st, lane->ev_drag, 0);  // join
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("lbm_advance: launch failed: %s", cudaGetErrorString(e));

@@ -58,6 +58,9 @@ struct alignas(16) FusedArgs {
   // drag/lift history
   double* drag_hist;
   long long drag_cap;
+  // 1: the drag kernel runs before the step advances the iteration counter;
+  // 2: after (on a second stream, beside the next step's bulk kernel)
+  int drag_it_offset;
   int n_obs;
   const int* obs_start;
   // outputs
@@ -698,7 +701,7 @@ __device__ __forceinline__ void special_collide(const FusedArgs& a, int s, int c
 __device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o) {
   const double* link_force = a.link_force;
   const int n_links = a.n_links;
-  long long slot = (*a.it_dev - 1) % a.drag_cap;
+  long long slot = (*a.it_dev - a.drag_it_offset) % a.drag_cap;
   if (slot < 0) slot += a.drag_cap;
   const int l0 = a.obs_start[o], l1 = a.obs_start[o + 1];
   double fx = 0.0, fy = 0.0;
@@ -735,4 +738,34 @@ __device__ __forceinline__ void drag_obstacle(const FusedArgs& a, int o) {
 namespace lbm {
 // Kernel arguments of one lattice from its C-ABI description (lbm_fused.cu).
 FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags);
+// Host: a second stream and two events per thread and device.  The drag/lift
+// sums of step k run on it beside the bulk kernel of step k + 1 (they read
+// only the per-link terms of step k, which the special-cell kernel of step
+// k + 1 overwrites after waiting for them); the caller's stream joins it at
+// the end of each enqueue.
+#ifndef LBM_DRAG_SIDE
+#define LBM_DRAG_SIDE 1  // 0: every kernel of a step on the caller's stream
+#endif
+struct DragLane {
+  cudaStream_t sd;
+  cudaEvent_t ev_special, ev_drag;
+};
+inline DragLane* drag_lane() {
+  thread_local DragLane lanes[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  DragLane& l = lanes[dev];
+  if (!l.sd) {
+    cudaStream_t sd = nullptr;
+    if (cudaStreamCreateWithFlags(&sd, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    if (cudaEventCreateWithFlags(&l.ev_special, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&l.ev_drag, cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamDestroy(sd);
+      return nullptr;
+    }
+    l.sd = sd;
+  }
+  return &l;
+}
+
 }  // namespace lbm
