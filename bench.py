@@ -332,12 +332,15 @@ def measure_sweep(steps):
     serial_g, _ = serial_loop_mlups(b, steps=50, graph=True)
     info = b.info()
     b.close()
-    k_trials = {t[0]["k_steps"]: t[1] for t in trials[-5:]}
+    k_trials = {t[0]["k_steps"]: t[1] for t in trials if t[0].get("_stage") == 2}
+    group_trials = {"%d groups, bulk_tma %d" % (t[0]["streams"], t[0].get("bulk_tma", 0)): t[1]
+                    for t in trials if t[0].get("_stage") == 3}
     return {"cases": info["lattices"], "cells": b.cells, "steps": steps, "mlups": mlups,
             "ms_per_step": ms / steps, "serial_loop_mlups": serial,
             "x_vs_serial": mlups / serial, "serial_graph_loop_mlups": serial_g,
             "x_vs_serial_graphs": mlups / serial_g, "config": best,
-            "k_steps_trials_mlups": k_trials, "setup_s": setup_s,
+            "k_steps_trials_mlups": k_trials, "concurrent_groups_trials_mlups": group_trials,
+            "setup_s": setup_s,
             "autotune_trials": len(trials), "precision": SWEEP_FORM,
             "all_finite": True}
 

@@ -288,8 +288,11 @@ typedef struct lbm_batch_config {
                                     widths of groups (a thread loops over them)   */
   int32_t bulk_tma;              /* 1 (16-bit forms only): the bulk phase runs the
                                     TMA-staged persistent kernel, on tiles of its
-                                    own size; bulk_threads, bulk_blocks_per_sm,
-                                    vec_bytes and tile_rounds then do not apply */
+                                    own size; 2: the same with half the warps per
+                                    block (two blocks per SM, room for another
+                                    batch's kernels beside them); bulk_threads,
+                                    bulk_blocks_per_sm, vec_bytes and tile_rounds
+                                    then do not apply                          */
 } lbm_batch_config;
 int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32_t n_cases,
                      const lbm_batch_config* cfg);

@@ -12,8 +12,14 @@
 * ``autotune(batch)``  picks the scheduling (persistent work queue or one
   block per tile), the vector width of the bulk kernel (cells per thread),
   block-widths per bulk tile,
-  threads per block, persistent grid size and the number of iterations per
-  CUDA graph by timing candidates on the batch.
+  threads per block, persistent grid size, the number of iterations per
+  CUDA graph and the number of concurrent groups by timing candidates on
+  the batch.
+
+With ``streams`` = n > 1 the lattices are split into n groups of about the
+same number of cells, each its own ``lbm_batch`` advanced on its own CUDA
+stream: the groups are independent, so the latency-bound special-cell
+phase of one group runs beside the bandwidth-bound bulk phase of another.
 """
 import contextlib
 import ctypes
@@ -142,44 +148,84 @@ class Batch:
         self.cells = sum(e.N for e in self.engines)
         self.it = 1          # next iteration to collide
         self.parity = 0      # every engine's f[0] holds g_up(0) after collide_from_g
-        self.handle = None
+        self.handles = []
+        self.streams = []
         self.config = None
         self.set_config(config or default_config())
 
+    @property
+    def handle(self):
+        """The lbm_batch of the first group (the only one with streams = 1)."""
+        return self.handles[0] if self.handles else None
+
+    def groups(self, n):
+        """Engine indices split into n groups of about the same number of
+        cells (largest lattice to the group with the fewest cells so far)."""
+        order = sorted(range(len(self.engines)), key=lambda i: -self.engines[i].N)
+        groups, cells = [[] for _ in range(n)], [0] * n
+        for i in order:
+            g = cells.index(min(cells))
+            groups[g].append(i)
+            cells[g] += self.engines[i].N
+        return [sorted(g) for g in groups if g]
+
+    def _destroy(self):
+        for h in self.handles:
+            _lib.call("lbm_batch_destroy", h)
+        self.handles = []
+
     def set_config(self, cfg):
-        if self.handle is not None:
-            _lib.call("lbm_batch_destroy", self.handle)
-            self.handle = None
+        self._destroy()
         self.config = dict(cfg)
-        arr = (_lib.Problem * len(self.engines))(*[e.P for e in self.engines])
+        n = int(cfg.get("streams", 1))
+        if n < 1:
+            raise ValueError("streams must be at least 1")
         c = _lib.BatchConfig(cfg["bulk_threads"], cfg["bulk_blocks_per_sm"],
                              cfg["special_blocks_per_sm"], cfg["scalar_tile_cells"],
                              int(cfg.get("persistent", 1)), int(cfg.get("vec_bytes", 16)),
                              int(cfg.get("tile_rounds", 1)), int(cfg.get("bulk_tma", 0)))
-        h = ctypes.c_void_p()
-        _lib.call("lbm_batch_create", ctypes.byref(h), arr, len(self.engines), ctypes.byref(c))
-        self.handle = h
+        for g in self.groups(n):
+            arr = (_lib.Problem * len(g))(*[self.engines[i].P for i in g])
+            h = ctypes.c_void_p()
+            _lib.call("lbm_batch_create", ctypes.byref(h), arr, len(g), ctypes.byref(c))
+            self.handles.append(h)
+        self.streams = [torch.cuda.Stream() for _ in self.handles] if len(self.handles) > 1 else []
 
     def info(self):
+        tot = {"lattices": 0, "bulk_tiles": 0, "special_tiles": 0, "drag_items": 0}
         out = (ctypes.c_int64 * 6)()
-        _lib.call("lbm_batch_info", self.handle, out)
-        return {"lattices": out[0], "bulk_tiles": out[1], "special_tiles": out[2],
-                "drag_items": out[3], "sms": out[4], "kernels_per_step": out[5]}
+        for h in self.handles:
+            _lib.call("lbm_batch_info", h, out)
+            for k, v in zip(("lattices", "bulk_tiles", "special_tiles", "drag_items"), out[:4]):
+                tot[k] += v
+        tot.update(sms=out[4], kernels_per_step=out[5], groups=len(self.handles))
+        return tot
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
     def advance(self, n_steps, graph=True, k=None):
-        """Advance every lattice by n_steps iterations, k per graph launch."""
+        """Advance every lattice by n_steps iterations, k per graph launch
+        (with several groups: each group's launches on its own stream, all
+        joined into the current stream at the end)."""
         k = k or self.config.get("k_steps", 50)
+        fn = "lbm_batch_advance_graph" if graph else "lbm_batch_advance"
+        cur = torch.cuda.current_stream()
+        for s in self.streams:
+            s.wait_stream(cur)
         done = 0
         while done < n_steps:
             n = min(k, n_steps - done)
-            fn = "lbm_batch_advance_graph" if graph else "lbm_batch_advance"
-            _lib.call(fn, self.handle, self.it, n, self.parity, self._stream())
+            if self.streams:
+                for h, s in zip(self.handles, self.streams):
+                    _lib.call(fn, h, self.it, n, self.parity, ctypes.c_void_p(s.cuda_stream))
+            else:
+                _lib.call(fn, self.handles[0], self.it, n, self.parity, self._stream())
             self.it += n
             self.parity ^= (n & 1)
             done += n
+        for s in self.streams:
+            cur.wait_stream(s)
         for e in self.engines:
             e.cur = self.parity
 
@@ -188,9 +234,7 @@ class Batch:
             e.check_status()
 
     def close(self):
-        if self.handle is not None:
-            _lib.call("lbm_batch_destroy", self.handle)
-            self.handle = None
+        self._destroy()
 
 
 # storage forms with a TMA-staged bulk kernel (lbm_batch_config.bulk_tma)
@@ -200,7 +244,7 @@ TMA_FORMS = ("f16s", "f16sr", "bf16s", "bf16sr")
 def default_config():
     return {"bulk_threads": 128, "bulk_blocks_per_sm": 8, "special_blocks_per_sm": 8,
             "scalar_tile_cells": 2048, "k_steps": 50, "persistent": 0, "vec_bytes": 8,
-            "tile_rounds": 4, "bulk_tma": 0}
+            "tile_rounds": 4, "bulk_tma": 0, "streams": 1}
 
 
 def time_batch(batch, n_steps, k=None):
@@ -215,14 +259,18 @@ def time_batch(batch, n_steps, k=None):
     return e0.elapsed_time(e1)
 
 
-def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200), verbose=False):
+def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200),
+             stream_space=(2, 3), verbose=False):
     """Pick the fastest batch configuration by timing candidates.
 
     Every candidate runs ``steps`` iterations after one warm-up launch (which
     also captures its graph); the lattices keep advancing, which does not
     change the cost per iteration.  A second stage times the winner with
     each number of iterations per CUDA graph in ``k_space`` (over the same
-    iteration count for every K).  Returns (best config, table of trials).
+    iteration count for every K), a third with the lattices split into each
+    number of concurrent groups in ``stream_space``.  Returns (best config,
+    table of trials); the trials of the second and third stages carry
+    ``_stage`` 2 and 3.
     """
     # one block per tile (the persistent grid size does not apply), then
     # persistent blocks, then (16-bit forms) the TMA-staged bulk kernel with
@@ -236,7 +284,7 @@ def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200), verbos
              "bulk_threads": [128], "bulk_blocks_per_sm": [8, 12], "k_steps": [50]},
         ]
         if batch.precision in TMA_FORMS:
-            space.append({"bulk_tma": [1], "persistent": [0, 1], "k_steps": [50]})
+            space.append({"bulk_tma": [1, 2], "persistent": [0, 1], "k_steps": [50]})
     spaces = [space] if isinstance(space, dict) else list(space)
     candidates = []
     for sp in spaces:
@@ -269,10 +317,29 @@ def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200), verbos
             batch.advance(k, k=k)  # warm-up + graph capture
             ms = time_batch(batch, n, k=k)
             mlups = batch.cells * n / (ms * 1e-3) / 1e6
-            trials.append((dict(cfg), mlups))
+            trials.append((dict(cfg, _stage=2), mlups))
             if verbose:
                 print(cfg, "%.0f MLUPS" % mlups)
             if best is None or mlups > best[1]:
+                best = (dict(cfg), mlups)
+    if stream_space:
+        k = best[0]["k_steps"]
+        n = k * max(1, -(-steps // k))
+        # with a TMA-staged bulk phase, both its shapes (the half-width one
+        # leaves room on each SM for the other groups' kernels)
+        bases = [dict(best[0])]
+        if best[0].get("bulk_tma"):
+            bases.append(dict(best[0], bulk_tma=3 - best[0]["bulk_tma"]))
+        for g, base in itertools.product(stream_space, bases):
+            cfg = dict(base, streams=g)
+            batch.set_config(cfg)
+            batch.advance(k, k=k)  # warm-up + graph capture
+            ms = time_batch(batch, n, k=k)
+            mlups = batch.cells * n / (ms * 1e-3) / 1e6
+            trials.append((dict(cfg, _stage=3), mlups))
+            if verbose:
+                print(cfg, "%.0f MLUPS" % mlups)
+            if mlups > best[1]:
                 best = (dict(cfg), mlups)
     batch.set_config(best[0])
     return best[0], trials

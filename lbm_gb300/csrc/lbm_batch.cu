@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128, LBM_SPECIAL_MIN_BLOCKS) k_batch_special(c
 // TMA-staged bulk phase: persistent blocks over every lattice's tiles (tiles
 // of the largest lattices first, taken round-robin by block).
 template <class St, class Sh>
-__global__ void __launch_bounds__(Sh::kThreads, 1) k_batch_bulk_tma(
+__global__ void __launch_bounds__(Sh::kThreads, Sh::kMinBlocks) k_batch_bulk_tma(
     const FusedArgs* __restrict__ args, const int4* __restrict__ tiles, int n_tiles,
     unsigned* queue, long long* it_dev, int last) {
   if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -166,6 +166,18 @@ __global__ void __launch_bounds__(256) k_batch_drag(const FusedArgs* __restrict_
     const int2 it = items[blockIdx.x];
     drag_obstacle(args[it.x], it.y);
   }
+}
+
+// The TMA-staged bulk phase: as many persistent blocks as fit on the GPU.
+template <class St, class Sh>
+void launch_batch_tma(const lbm_batch* b, const FusedArgs* args, int last, cudaStream_t st) {
+  static int per_sm[64] = {};
+  const int slots =
+      tma_prepare((const void*)k_batch_bulk_tma<St, Sh>, Sh::kThreads, Sh::kSmem, per_sm) *
+      b->sm_count;
+  k_batch_bulk_tma<St, Sh><<<b->n_bulk_tiles < slots ? b->n_bulk_tiles : slots, Sh::kThreads,
+                             Sh::kSmem, st>>>(args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue,
+                                              b->d_it, last);
 }
 
 template <class St, int VB, bool kVecOnly>
@@ -199,14 +211,12 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
     const FusedArgs* args = b->d_args + (size_t)((parity + k) & 1) * b->n_cases;
     if constexpr (sizeof(typename St::S) == 2 && St::kShift) {
       if (b->cfg.bulk_tma) {
-        using Sh = typename TmaShapeOf<St>::type;
-        static int per_sm[64] = {};
-        const int slots =
-            tma_prepare((const void*)k_batch_bulk_tma<St, Sh>, Sh::kThreads, Sh::kSmem, per_sm) *
-            b->sm_count;
-        k_batch_bulk_tma<St, Sh>
-            <<<b->n_bulk_tiles < slots ? b->n_bulk_tiles : slots, Sh::kThreads, Sh::kSmem, st>>>(
-                args, b->d_bulk_tiles, b->n_bulk_tiles, b->d_queue, b->d_it, bulk_last);
+        using Full = typename TmaShapeOf<St>::type;
+        using Half = typename TmaHalf<Full>::type;
+        if (b->cfg.bulk_tma == 2)
+          launch_batch_tma<St, Half>(b, args, bulk_last, st);
+        else
+          launch_batch_tma<St, Full>(b, args, bulk_last, st);
         if (special) {
           wait_drag();
           if (b->cfg.persistent)
@@ -309,7 +319,7 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       cfg->scalar_tile_cells < 32 || cfg->scalar_tile_cells > (1 << 20) ||
       (cfg->persistent != 0 && cfg->persistent != 1) ||
       (cfg->vec_bytes != 8 && cfg->vec_bytes != 16) || cfg->tile_rounds < 1 ||
-      cfg->tile_rounds > 64 || (cfg->bulk_tma != 0 && cfg->bulk_tma != 1)) {
+      cfg->tile_rounds > 64 || cfg->bulk_tma < 0 || cfg->bulk_tma > 2) {
     set_error("lbm_batch_create: bad config (threads %d, blocks/SM %d/%d, tile %d)",
               cfg->bulk_threads, cfg->bulk_blocks_per_sm, cfg->special_blocks_per_sm,
               cfg->scalar_tile_cells);
@@ -326,7 +336,7 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
   const int V = (prec == LBM_PREC_F64 || prec == LBM_PREC_Q60)
                     ? 1
                     : cfg->vec_bytes / (prec == LBM_PREC_F32 ? 4 : 2);
-  const int tma_cells = cfg->bulk_tma ? tma_tile_cells(prec) : 0;
+  const int tma_cells = cfg->bulk_tma ? tma_tile_cells(prec, cfg->bulk_tma == 2) : 0;
   if (cfg->bulk_tma && !tma_cells) {
     set_error("lbm_batch_create: bulk_tma needs a 16-bit storage form");
     return LBM_ERR_ARG;

@@ -301,12 +301,18 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
   return LBM_OK;
 }
 
-int tma_tile_cells(int precision) {
+template <class St>
+static int tile_cells_of(bool half) {
+  using Sh = typename TmaShapeOf<St>::type;
+  return half ? TmaHalf<Sh>::type::kCells : Sh::kCells;
+}
+
+int tma_tile_cells(int precision, bool half) {
   switch (precision) {
-    case LBM_PREC_F16S: return TmaShapeOf<StoreF16>::type::kCells;
-    case LBM_PREC_F16SR: return TmaShapeOf<StoreF16SR>::type::kCells;
-    case LBM_PREC_BF16S: return TmaShapeOf<StoreBF16>::type::kCells;
-    case LBM_PREC_BF16SR: return TmaShapeOf<StoreBF16SR>::type::kCells;
+    case LBM_PREC_F16S: return tile_cells_of<StoreF16>(half);
+    case LBM_PREC_F16SR: return tile_cells_of<StoreF16SR>(half);
+    case LBM_PREC_BF16S: return tile_cells_of<StoreBF16>(half);
+    case LBM_PREC_BF16SR: return tile_cells_of<StoreBF16SR>(half);
     default: return 0;
   }
 }

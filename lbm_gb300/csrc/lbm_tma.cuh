@@ -34,10 +34,11 @@ constexpr int kTmaBarBytes = 128;  // the stages' mbarriers
 constexpr unsigned long long kWaitNs = 500ull * 1000 * 1000;
 
 // Shape of the kernel: W consumer warps of V cells per thread (tiles of
-// W * 32 * V cells), NST stages, plus one producer warp.
-template <int W, int V, int NST>
+// W * 32 * V cells), NST stages, plus one producer warp; compiled for MB
+// resident blocks per SM.
+template <int W, int V, int NST, int MB = 1>
 struct TmaShape {
-  static constexpr int kWarps = W, kV = V, kStages = NST;
+  static constexpr int kWarps = W, kV = V, kStages = NST, kMinBlocks = MB;
   static constexpr int kConsumers = W * 32;
   static constexpr int kThreads = kConsumers + 32;
   static constexpr int kCells = kConsumers * V;
@@ -73,6 +74,13 @@ struct TmaShapeOf<StoreBF16> {
   using type = TmaShape<12, 4, 6>;
 };
 #endif
+// Half the consumer warps of the form's shape (tiles half as long, half the
+// shared memory): two blocks per SM, which leaves room for the blocks of
+// another batch's kernels beside them (batches advanced concurrently).
+template <class Sh>
+struct TmaHalf {
+  using type = TmaShape<Sh::kWarps / 2, Sh::kV, Sh::kStages, 2>;
+};
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -300,7 +308,8 @@ inline int tma_prepare(const void* kernel, int threads, size_t smem, int* cache)
   return cache[dev];
 }
 
-// Cells per tile of the form's TMA-staged kernel (0: the form has none).
-int tma_tile_cells(int precision);
+// Cells per tile of the form's TMA-staged kernel (half: of its half-width
+// shape; 0: the form has none).
+int tma_tile_cells(int precision, bool half = false);
 
 }  // namespace lbm

@@ -39,24 +39,29 @@ def _finish(batch, steps):
 
 # persistent: 1 work-queue kernels, 0 one block per tile; rounds: block-widths
 # of vector groups per bulk tile; tma: the TMA-staged bulk kernel (16-bit
-# forms; the single lattices step through it too, so this also compares the
-# two bulk kernels where tma is 0).
-@pytest.mark.parametrize("precision,persistent,vec_bytes,rounds,tma", [
-    ("f16s", 1, 16, 1, 0), ("f64", 1, 16, 1, 0), ("f16sr", 0, 8, 1, 0), ("f16sr", 1, 8, 4, 0),
-    ("f16sr", 0, 16, 3, 0), ("q60", 0, 16, 1, 0), ("f16s", 1, 16, 1, 1), ("f16sr", 0, 16, 1, 1),
-    ("bf16s", 0, 16, 1, 1), ("bf16sr", 1, 16, 1, 1)])
-def test_batch_equals_single_lattices(cuda, precision, persistent, vec_bytes, rounds, tma):
+# forms; 1 the form's shape, 2 half its warps per block; the single lattices
+# step through the TMA-staged kernel too, so this also compares the two bulk
+# kernels where tma is 0); groups: lattices split into that many batches
+# advanced concurrently on their own streams.
+@pytest.mark.parametrize("precision,persistent,vec_bytes,rounds,tma,groups", [
+    ("f16s", 1, 16, 1, 0, 1), ("f64", 1, 16, 1, 0, 1), ("f16sr", 0, 8, 1, 0, 1),
+    ("f16sr", 1, 8, 4, 0, 1), ("f16sr", 0, 16, 3, 0, 1), ("q60", 0, 16, 1, 0, 1),
+    ("f16s", 1, 16, 1, 1, 1), ("f16sr", 0, 16, 1, 1, 1), ("bf16s", 0, 16, 1, 1, 1),
+    ("bf16sr", 1, 16, 1, 1, 1), ("f16sr", 0, 16, 1, 1, 2), ("q60", 0, 16, 1, 0, 3),
+    ("f16s", 0, 16, 1, 2, 2), ("bf16sr", 1, 16, 1, 2, 1)])
+def test_batch_equals_single_lattices(cuda, precision, persistent, vec_bytes, rounds, tma,
+                                      groups):
     steps = 120
     cfg = default_config()
     cfg.update(persistent=persistent, vec_bytes=vec_bytes, bulk_threads=64, tile_rounds=rounds,
-               bulk_tma=tma)
+               bulk_tma=tma, streams=groups)
     b = Batch(_apps(), precision=precision, config=cfg)
     b.advance(steps, k=40)
     b.check()
     got = _finish(b, steps)
     info = b.info()
     b.close()
-    assert info["lattices"] == 5 and info["drag_items"] == 3
+    assert info["lattices"] == 5 and info["drag_items"] == 3 and info["groups"] == groups
 
     s = Batch(_apps(), precision=precision)
     for eng in s.engines:
