@@ -5,7 +5,9 @@ buffers of post-collision populations in the storage form (``f64``, ``q60``,
 ``f32``, ``f16s``, ``bf16s``, ``f16sr``, ``bf16sr``), the special-cell and link tables, the scratch that the
 kernels carry from one iteration to the next, the per-iteration drag/lift
 history and the BC schedule.  It drives ``lbm_advance`` /
-``lbm_advance_graph`` of liblbm_gb300 (include/lbm_gb300.h).
+``lbm_advance_graph`` of liblbm_gb300 (include/lbm_gb300.h).  The 16-bit
+forms step through the TMA-staged bulk kernel; ``bulk_kernel = "registers"``
+selects the register-pipelined one (``LBM_FLAG_BULK_REGISTERS``, same bits).
 
 Iteration numbering follows lbm/src/core/run.py: iteration ``it`` computes
 macro, equilibrium and collision of g(it); its boundary conditions and its
