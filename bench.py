@@ -246,25 +246,31 @@ def measure_form(ny, precision, steps, warmup, tmp, peak_gbs, dist=None):
     return res, (app, lat, eng, it)
 
 
-def measure_e2e(app, lat, eng, it, steps):
+def measure_e2e(app, lat, eng, it, steps, depth=2):
     """Step by step through the C-ABI with host buffers: every step's BC
     vectors go up from pinned host memory and every step's drag/lift of all
-    obstacles comes back to pinned host memory and is read by the host.  One
-    step deep pipeline: step k + 1 (its BC vectors computed on the host and
-    copied into the other of two device buffers) is enqueued before the host
-    waits for step k's drag/lift, so the GPU does not idle while the host
-    turns around."""
+    obstacles comes back to pinned host memory and is read by the host.
+    The copies run on a copy stream (each step's kernels wait for its
+    upload; each download waits for its step), and the host runs ``depth``
+    steps ahead: step k + depth (its BC vectors computed on the host and
+    copied into one of depth + 1 rotating device buffers) is enqueued before
+    the host waits for step k's drag/lift, so neither the copies nor the
+    host's turnaround leave the GPU idle."""
     import torch
     nx, ny = lat.nx, lat.ny
     base, vec, scale = app.bc_schedule(lat)
     n_obs = len(eng.obstacles)
-    h_bc = [torch.empty(base.size, dtype=torch.float64).pin_memory() for _ in range(2)]
-    d_bc = [eng.bc_base, torch.empty_like(eng.bc_base)]
-    h_drag = [torch.empty((n_obs, 2), dtype=torch.float64).pin_memory() for _ in range(2)]
-    done = [torch.cuda.Event(), torch.cuda.Event()]
+    nb = depth + 1
+    h_bc = [torch.empty(base.size, dtype=torch.float64).pin_memory() for _ in range(nb)]
+    d_bc = [eng.bc_base] + [torch.empty_like(eng.bc_base) for _ in range(nb - 1)]
+    h_drag = [torch.empty((n_obs, 2), dtype=torch.float64).pin_memory() for _ in range(nb)]
+    up = [torch.cuda.Event() for _ in range(nb)]      # upload of buffer b done
+    ran = [torch.cuda.Event() for _ in range(nb)]     # step using buffer b done
+    down = [torch.cuda.Event() for _ in range(nb)]    # drag/lift of buffer b on the host
     eng.set_bc_constant(base)
     P = eng.P
     stream = torch.cuda.current_stream()
+    copy = torch.cuda.Stream()
 
     def host_bc(m, buf):  # BC vectors of iteration m - 1, straight into pinned memory
         hb = buf.numpy()
@@ -272,16 +278,24 @@ def measure_e2e(app, lat, eng, it, steps):
         np.add(hb, base, out=hb)
 
     def launch(m, b):  # step m with BC buffer b, then its drag/lift down into h_drag[b]
+        up[b].synchronize()  # the pinned buffer's previous upload has been read
         host_bc(m, h_bc[b])
-        d_bc[b].copy_(h_bc[b], non_blocking=True)
+        with torch.cuda.stream(copy):
+            copy.wait_event(ran[b])  # the device buffer's previous step is done
+            d_bc[b].copy_(h_bc[b], non_blocking=True)
+            up[b].record(copy)
+        stream.wait_event(up[b])
         P.bc_base = d_bc[b].data_ptr()
         eng.steps(m, 1, graph=True)
+        ran[b].record(stream)
         slot = (m - 1) % eng.drag_cap
-        h_drag[b].copy_(eng.drag_hist[slot, :n_obs], non_blocking=True)
-        done[b].record(stream)
+        with torch.cuda.stream(copy):
+            copy.wait_event(ran[b])
+            h_drag[b].copy_(eng.drag_hist[slot, :n_obs], non_blocking=True)
+            down[b].record(copy)
 
-    # two untimed steps capture the one-step graphs of both BC buffers
-    for k in range(2):
+    # untimed steps capture the one-step graph of every BC buffer
+    for k in range(nb):
         launch(it, k)
         it += 1
     torch.cuda.synchronize()
@@ -291,12 +305,14 @@ def measure_e2e(app, lat, eng, it, steps):
     e0.record(stream)
     checksum = 0.0
     for k in range(steps):
-        launch(it + k, k & 1)
-        if k > 0:  # step k - 1's drag/lift on the host
-            done[(k - 1) & 1].synchronize()
-            checksum += float(h_drag[(k - 1) & 1].numpy().sum())
-    done[(steps - 1) & 1].synchronize()
-    checksum += float(h_drag[(steps - 1) & 1].numpy().sum())
+        launch(it + k, k % nb)
+        if k >= depth:  # step k - depth's drag/lift on the host
+            down[(k - depth) % nb].synchronize()
+            checksum += float(h_drag[(k - depth) % nb].numpy().sum())
+    for k in range(max(0, steps - depth), steps):
+        down[k % nb].synchronize()
+        checksum += float(h_drag[k % nb].numpy().sum())
+    stream.wait_stream(copy)
     e1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -306,22 +322,24 @@ def measure_e2e(app, lat, eng, it, steps):
         raise FloatingPointError("end-to-end run: non-finite drag/lift")
     return {"value": nx * ny * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS",
             "h2d_bytes_per_step": int(base.size * 8), "d2h_bytes_per_step": int(n_obs * 2 * 8),
-            "wall_s": wall, "steps": steps, "pipeline_depth": 1}
+            "wall_s": wall, "steps": steps, "pipeline_depth": depth}
 
 
 def measure_sweep(steps):
     """The 256-case sweep (FP16 shifted storage): autotune (scheduling,
-    vector width, threads, tile rounds, then iterations per graph), then
-    `steps` iterations of every case in batched graphs; the per-case serial
-    loop is timed for comparison, with plain launches (20 iterations) and
-    with one CUDA graph per case (50 iterations)."""
+    vector width, threads, tile rounds, bulk kernel, then iterations per
+    graph and concurrent groups; the lattices are put back in their state
+    before the trials), then `steps` iterations of every case in batched
+    graphs; the per-case serial loop is timed for comparison, with plain
+    launches (20 iterations) and with one CUDA graph per case (50
+    iterations)."""
     import torch
     from lbm_gb300.batch import Batch, autotune, serial_loop_mlups, sweep_apps, time_batch
     t0 = time.perf_counter()
-    # BC schedule length: the timed iterations, the autotuner's trials
-    # (20 configurations x 250 iterations, then 5 x (K + 200)) and the
-    # serial loops.
-    b = Batch(sweep_apps(seed=2024), precision=SWEEP_FORM, max_steps=steps + 10000)
+    # BC schedule length: the autotuner's trials (24 configurations x 250
+    # iterations, then 5 x (K + 200) and 4 x (K + 200), rolled back
+    # afterwards), the timed iterations and the serial loops.
+    b = Batch(sweep_apps(seed=2024), precision=SWEEP_FORM, max_steps=steps + 12000)
     setup_s = time.perf_counter() - t0
     best, trials = autotune(b, steps=200)
     b.check()

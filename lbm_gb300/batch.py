@@ -270,8 +270,12 @@ def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200),
     iteration count for every K), a third with the lattices split into each
     number of concurrent groups in ``stream_space``.  Returns (best config,
     table of trials); the trials of the second and third stages carry
-    ``_stage`` 2 and 3.
+    ``_stage`` 2 and 3.  The lattices are put back in the state they had
+    before the trials (the sweep's channels at tau = 0.53 go unstable after
+    ~17,000 iterations, so the trials must not age them).
     """
+    snaps = [e.snapshot() for e in batch.engines]
+    it0, parity0 = batch.it, batch.parity
     # one block per tile (the persistent grid size does not apply), then
     # persistent blocks, then (16-bit forms) the TMA-staged bulk kernel with
     # either schedule of the special cells; a dict of value lists or a list
@@ -342,6 +346,11 @@ def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200),
             if mlups > best[1]:
                 best = (dict(cfg), mlups)
     batch.set_config(best[0])
+    torch.cuda.synchronize()
+    for e, snap in zip(batch.engines, snaps):
+        e.restore(snap)
+    batch.it, batch.parity = it0, parity0
+    torch.cuda.synchronize()
     return best[0], trials
 
 

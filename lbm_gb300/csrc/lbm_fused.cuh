@@ -121,6 +121,9 @@ __device__ __forceinline__ double bc_value(const FusedArgs& a, double s, int off
 // integer collision (collide_q60), store the 9 integers.  A cell outside the
 // range of the form stores kQ60Bad (NaN when converted back) and sets status
 // bit 0 when finite checks are on.
+__device__ __forceinline__ void q60_collide_store(const FusedArgs& a, int i, int j,
+                                                  long long cell, long long (&x)[9]);
+
 __device__ __forceinline__ void bulk_q60_ij(const FusedArgs& a, int i, int j) {
   if (i <= 0 || i >= a.nx - 1 || j <= 0 || j >= a.ny - 1) return;
   const long long Ns = a.Ns, sy = a.sy;
@@ -136,6 +139,14 @@ __device__ __forceinline__ void bulk_q60_ij(const FusedArgs& a, int i, int j) {
   x[6] = __ldg(fin + 6 * Ns + cell + sy + 1);
   x[7] = __ldg(fin + 7 * Ns + cell + sy - 1);
   x[8] = __ldg(fin + 8 * Ns + cell - sy + 1);
+  q60_collide_store(a, i, j, cell, x);
+}
+
+// Integer collision of interior cell (i, j) from its nine pulled populations
+// and the stores (shared by the register-pipelined and TMA-staged kernels).
+__device__ __forceinline__ void q60_collide_store(const FusedArgs& a, int i, int j,
+                                                  long long cell, long long (&x)[9]) {
+  const long long Ns = a.Ns;
   long long rho, jx, jy;
   const bool ok = collide_q60(x, a.kq, rho, jx, jy);
   if (a.write_macro) {

@@ -29,20 +29,21 @@
 
 namespace lbm {
 
-constexpr int kTmaHalo = 8;        // one 16-byte vector of 16-bit elements
 constexpr int kTmaBarBytes = 128;  // the stages' mbarriers
 constexpr unsigned long long kWaitNs = 500ull * 1000 * 1000;
 
 // Shape of the kernel: W consumer warps of V cells per thread (tiles of
 // W * 32 * V cells), NST stages, plus one producer warp; compiled for MB
-// resident blocks per SM.
+// resident blocks per SM.  Each plane's copy is widened by kHalo elements
+// (16 bytes) on either side.
 template <int W, int V, int NST, int MB = 1>
 struct TmaShape {
   static constexpr int kWarps = W, kV = V, kStages = NST, kMinBlocks = MB;
   static constexpr int kConsumers = W * 32;
   static constexpr int kThreads = kConsumers + 32;
   static constexpr int kCells = kConsumers * V;
-  static constexpr int kRow = kCells + 2 * kTmaHalo;  // elements per plane and stage
+  static constexpr int kHalo = 8;
+  static constexpr int kRow = kCells + 2 * kHalo;  // elements per plane and stage
   // barriers | one FusedArgs per stage (batched tiles) | stages
   static constexpr size_t kArgsBytes = (size_t)NST * sizeof(FusedArgs);
   static constexpr size_t kSmem = kTmaBarBytes + kArgsBytes + (size_t)NST * 9 * kRow * 2;
@@ -138,11 +139,11 @@ struct TmaRange {
   int dst;
 };
 __device__ __forceinline__ TmaRange tma_range(int q, long long c0, long long len, int sy,
-                                              long long Ns) {
-  const long long s0 = c0 - (long long)cx(q) * sy - kTmaHalo;
+                                              long long Ns, int halo) {
+  const long long s0 = c0 - (long long)cx(q) * sy - halo;
   TmaRange r;
   r.lo = s0 < 0 ? 0 : s0;
-  const long long h = s0 + len + 2 * kTmaHalo;
+  const long long h = s0 + len + 2 * halo;
   r.hi = h > Ns ? Ns : h;
   r.dst = (int)(r.lo - s0);
   return r;
@@ -181,6 +182,66 @@ struct BatchTiles {
   __device__ __forceinline__ int count(int t) const { return tiles[t].z; }
 };
 
+// Barrier set-up of a TMA-staged block: a `full` mbarrier per stage (one
+// arrival, the producer's, plus the copies' bytes) and an `empty` one (one
+// arrival per consumer thread).  Every thread calls it.
+template <class Sh>
+__device__ __forceinline__ void tma_init(unsigned full0, unsigned empty0) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Sh::kStages; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, Sh::kConsumers);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// The producer thread: for tile k of this block, wait until the consumers
+// have released stage k % NST, then copy the tile's nine source ranges (and,
+// with Src::kStageArgs, its FusedArgs) into it.
+template <class S, class Sh, class Src>
+__device__ __forceinline__ void tma_produce(const Src& src, int n_tiles, unsigned* status,
+                                            unsigned full0, unsigned empty0, S* stage,
+                                            FusedArgs* stage_args) {
+  constexpr int NST = Sh::kStages, kRow = Sh::kRow;
+  constexpr bool kStageArgs = Src::kStageArgs;
+  int k = 0;
+  bool ok = true;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
+    const int s = k % NST;
+    if (k >= NST && !mbar_wait(empty0 + 8 * s, ((k / NST) - 1) & 1)) {
+      ok = false;
+      break;
+    }
+    const FusedArgs& a = src.args(t);
+    const S* fin = (const S*)a.fin;
+    const long long Ns = a.Ns, c0 = src.first(t);
+    const int sy = a.sy, len = src.count(t);
+    unsigned bytes = kStageArgs ? (unsigned)sizeof(FusedArgs) : 0u;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const TmaRange r = tma_range(q, c0, len, sy, Ns, Sh::kHalo);
+      bytes += (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S);
+    }
+    mbar_expect_tx(full0 + 8 * s, bytes);
+    if (kStageArgs)
+      bulk_load(smem_addr(stage_args + s), &a, (unsigned)sizeof(FusedArgs), full0 + 8 * s);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const TmaRange r = tma_range(q, c0, len, sy, Ns, Sh::kHalo);
+      bulk_load(smem_addr(stage + (size_t)(s * 9 + q) * kRow + r.dst), fin + q * Ns + r.lo,
+                (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S), full0 + 8 * s);
+    }
+  }
+  if (!ok) {
+    if (status) atomicOr(status, 8u);
+    // the copies of the last issued tiles may still be in flight
+    for (int kk = k - NST < 0 ? 0 : k - NST; kk < k; ++kk)
+      mbar_wait(full0 + 8 * (kk % NST), (kk / NST) & 1);
+  }
+}
+
 // The kernel body; every thread of the block calls it.  status: where a
 // timed-out wait is reported.
 template <class St, class Sh, class Src>
@@ -188,6 +249,7 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
   using S = typename St::S;
   using T = typename St::T;
   constexpr int V = Sh::kV, NST = Sh::kStages, kConsumers = Sh::kConsumers, kRow = Sh::kRow;
+  constexpr int kHalo = Sh::kHalo;
   using P = Pack<S, V>;
   static_assert(sizeof(S) == 2, "16-bit storage forms only");
   constexpr bool kStageArgs = Src::kStageArgs;
@@ -196,50 +258,9 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
   FusedArgs* stage_args = reinterpret_cast<FusedArgs*>(smem + kTmaBarBytes);
   S* stage = reinterpret_cast<S*>(smem + kTmaBarBytes + Sh::kArgsBytes);
   const int tid = threadIdx.x;
-  if (tid == 0) {
-    for (int s = 0; s < NST; ++s) {
-      mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, kConsumers);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
+  tma_init<Sh>(full0, empty0);
   if (tid == kConsumers) {
-    // producer
-    int k = 0;
-    bool ok = true;
-    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
-      const int s = k % NST;
-      if (k >= NST && !mbar_wait(empty0 + 8 * s, ((k / NST) - 1) & 1)) {
-        ok = false;
-        break;
-      }
-      const FusedArgs& a = src.args(t);
-      const S* fin = (const S*)a.fin;
-      const long long Ns = a.Ns, c0 = src.first(t);
-      const int sy = a.sy, len = src.count(t);
-      unsigned bytes = kStageArgs ? (unsigned)sizeof(FusedArgs) : 0u;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        const TmaRange r = tma_range(q, c0, len, sy, Ns);
-        bytes += (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S);
-      }
-      mbar_expect_tx(full0 + 8 * s, bytes);
-      if (kStageArgs)
-        bulk_load(smem_addr(stage_args + s), &a, (unsigned)sizeof(FusedArgs), full0 + 8 * s);
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        const TmaRange r = tma_range(q, c0, len, sy, Ns);
-        bulk_load(smem_addr(stage + (size_t)(s * 9 + q) * kRow + r.dst), fin + q * Ns + r.lo,
-                  (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S), full0 + 8 * s);
-      }
-    }
-    if (!ok) {
-      if (status) atomicOr(status, 8u);
-      // the copies of the last issued tiles may still be in flight
-      for (int kk = k - NST < 0 ? 0 : k - NST; kk < k; ++kk)
-        mbar_wait(full0 + 8 * (kk % NST), (kk / NST) & 1);
-    }
+    tma_produce<S, Sh>(src, n_tiles, status, full0, empty0, stage, stage_args);
   } else if (tid < kConsumers) {
     int k = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
@@ -259,7 +280,7 @@ __device__ __forceinline__ void bulk_tma_body(const Src& src, int n_tiles, unsig
       T halo[9];
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
-        const S* row = stage + (size_t)(s * 9 + q) * kRow + kTmaHalo + off;
+        const S* row = stage + (size_t)(s * 9 + q) * kRow + kHalo + off;
         if (act) in[q] = *reinterpret_cast<const P*>(row);
         if (cy(q) == 1)  // cell j0 pulls from j0 - 1 (zero at a column start)
           halo[q] = act && j0 > 0 ? St::load(row - 1) : T(0);
