@@ -569,8 +569,18 @@ def measure_app_api(steps, tmp, engine_mlups, ny=200):
     moving averages and convergence test, one drag_lift line per iteration),
     wall time from run() to its return, against the engine-only figure of
     the same case (run_case).  Field outputs are off (output_freq beyond the
-    run): they are the app's file writes, not the lattice update."""
+    run): they are the app's file writes, not the lattice update.  An untimed
+    2,000-iteration run first loads what a process loads once (the CUDA
+    modules of the PyTorch operations the hooks use, the buffers' code
+    paths): measured at ~2 s, which is not a per-run cost."""
     import lbm_gb300
+    warm = channel_app(ny, 2000)
+    wout = tempfile.mkdtemp(prefix="app_api_warm_", dir=tmp)
+    with contextlib.redirect_stdout(io.StringIO()):
+        wlat = lbm_gb300.lattice(warm, precision="q60", output_dir=wout + "/", verbose=False)
+        wlat.generate_image = lambda obstacles: None
+        lbm_gb300.run(wlat, warm)
+    del wlat
     app = channel_app(ny, steps)
     out = tempfile.mkdtemp(prefix="app_api_", dir=tmp)
     with contextlib.redirect_stdout(io.StringIO()):

@@ -190,7 +190,7 @@ void enqueue_store_vb(const lbm_batch* b, int n_steps, int parity, cudaStream_t 
   // by the special phase of k + 1, which rewrites the per-link terms.
   const bool drag = b->n_drag_items > 0, special = b->n_special_tiles > 0;
   const int bulk_last = !special, special_last = special;
-  DragLane* lane = drag && LBM_DRAG_SIDE ? drag_lane() : nullptr;
+  DragLane* lane = drag && LBM_DRAG_SIDE && n_steps > 1 ? drag_lane() : nullptr;
   bool drag_pending = false;
   auto wait_drag = [&]() {
     if (drag_pending) cudaStreamWaitEvent(st, lane->ev_drag, 0);

@@ -273,8 +273,10 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
                   unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev) {
   FusedArgs a = make_args(p, mode, flags);
   if (set_it) k_set_it<<<1, 1, 0, st>>>(a.it_dev, a.step_done, it0);
-  // per-kernel timing (ev) keeps every kernel on st
-  DragLane* lane = ev || !LBM_DRAG_SIDE ? nullptr : drag_lane();
+  // per-kernel timing (ev) keeps every kernel on st, and so does a single
+  // step (its drag kernel has no next bulk kernel to run beside before the
+  // join)
+  DragLane* lane = ev || !LBM_DRAG_SIDE || n_steps < 2 ? nullptr : drag_lane();
   bool drag_pending = false;
   for (int k = 0; k < n_steps; ++k) {
     const int par = (parity + k) & 1;  // f[par] holds g_up of the previous iteration
