@@ -227,6 +227,11 @@ typedef struct lbm_problem {
  * loads, warp-shuffle halos) instead of the default TMA-staged one
  * (cp.async.bulk into shared-memory stages); both give the same bits. */
 #define LBM_FLAG_BULK_REGISTERS 8u
+/* Test of the failure path only: the TMA-staged kernel's producer withholds
+ * each block's first tile, so that the consumers' bounded wait (0.5 s) runs
+ * out; the kernel then sets status bit 3 and returns, and the context stays
+ * usable.  No result of such a step is meaningful. */
+#define LBM_FLAG_TEST_STALL 16u
 
 size_t lbm_problem_scratch_bytes(const lbm_problem* p);
 /* Advance n_steps iterations: each is one pass of the reference's run() loop

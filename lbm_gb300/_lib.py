@@ -30,6 +30,7 @@ CORNER_BOTTOM_LEFT, CORNER_TOP_LEFT, CORNER_TOP_RIGHT, CORNER_BOTTOM_RIGHT = 0, 
 
 MODE_COLLIDE_FROM_G, MODE_STEP, MODE_FINISH = 0, 1, 2
 FLAG_MACRO_LAST, FLAG_CHECK_FINITE, FLAG_WALL_MACRO, FLAG_BULK_REGISTERS = 1, 2, 4, 8
+FLAG_TEST_STALL = 16
 
 
 class LbmError(RuntimeError):

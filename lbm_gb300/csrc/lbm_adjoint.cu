@@ -692,8 +692,25 @@ int adjoint_args_check(const lbm_problem* p, const lbm_adjoint* adj, const char*
 }
 
 // Enqueue adjoint step `it` (checked arguments).
-int adjoint_enqueue(const lbm_problem* p, const lbm_adjoint* adj, int64_t it, const double* x_prev,
-                    const double* lam_in, double* lam_out, cudaStream_t st, const char* fn) {
+// The arguments of the adjoint step that do not change from step to step.
+void adjoint_prepare(const lbm_problem* p, const lbm_adjoint* adj, AdjArgs& A) {
+  memset(&A, 0, sizeof(A));
+  A.f = make_args(p, LBM_MODE_STEP, 0);
+  A.k = make_rates(p->om_p, p->om_m, 0.25);
+  A.adj_pulled = adj->adj_pulled;
+  A.link_adj = adj->link_adj;
+  A.corner_seed = adj->corner_seed;
+  A.grad_bc_base = adj->grad_bc_base;
+  A.grad_bc_vec = adj->grad_bc_vec;
+  A.grad_omega = adj->grad_omega;
+  A.is_special = adj->is_special;
+  A.obj_w = adj->obj_w;
+}
+
+// One adjoint step (iteration it) with the prepared arguments.
+int adjoint_launch(const lbm_problem* p, const lbm_adjoint* adj, AdjArgs& A, int64_t it,
+                   const double* x_prev, const double* lam_in, double* lam_out, cudaStream_t st,
+                   const char* fn) {
   if (!x_prev || !lam_in || !lam_out || it < 1) {
     set_error("%s: bad arguments", fn);
     return LBM_ERR_ARG;
@@ -702,31 +719,26 @@ int adjoint_enqueue(const lbm_problem* p, const lbm_adjoint* adj, int64_t it, co
     set_error("%s: BC scale table does not cover iteration %lld", fn, (long long)it - 1);
     return LBM_ERR_ARG;
   }
-  AdjArgs A;
-  memset(&A, 0, sizeof(A));
-  A.f = make_args(p, LBM_MODE_STEP, 0);
   A.f.fin = x_prev;
-  A.k = make_rates(p->om_p, p->om_m, 0.25);
   A.lam_in = lam_in;
   A.lam_out = lam_out;
-  A.adj_pulled = adj->adj_pulled;
-  A.link_adj = adj->link_adj;
-  A.corner_seed = adj->corner_seed;
-  A.grad_bc_base = adj->grad_bc_base;
-  A.grad_bc_vec = adj->grad_bc_vec;
-  A.grad_omega = adj->grad_omega;
+  A.it = it;
+  A.in_window = (it - 1 >= adj->obj_it_first && it - 1 <= adj->obj_it_last) ? 1 : 0;
   const long long N = (long long)p->nx * p->ny;
   const int nbb = (int)((N + 127) / 128);
   const int nbs = (p->n_special + 3) / 4;  // one warp per special cell
-  A.is_special = adj->is_special;
-  A.obj_w = adj->obj_w;
-  A.it = it;
-  A.in_window = (it - 1 >= adj->obj_it_first && it - 1 <= adj->obj_it_last) ? 1 : 0;
   k_adj_cells<<<nbb + nbs + 1, 128, 0, st>>>(A, nbb, nbs);
   k_adj_gather<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(A);
   if (p->n_links > 0) k_adj_links<<<(p->n_links + 255) / 256, 256, 0, st>>>(A);
   LBM_CUDA_CHECK(cudaGetLastError(), fn);
   return LBM_OK;
+}
+
+int adjoint_enqueue(const lbm_problem* p, const lbm_adjoint* adj, int64_t it, const double* x_prev,
+                    const double* lam_in, double* lam_out, cudaStream_t st, const char* fn) {
+  AdjArgs A;
+  adjoint_prepare(p, adj, A);
+  return adjoint_launch(p, adj, A, it, x_prev, lam_in, lam_out, st, fn);
 }
 }  // namespace
 
@@ -753,15 +765,7 @@ extern "C" int lbm_adjoint_recompute(const lbm_problem* p, int64_t it_first, int
   }
   // Each step reads one slot and writes the next; no drag history (the
   // objective is known from the forward run).
-  lbm_problem q = *p;
-  q.drag_hist = nullptr;
-  cudaStream_t st = (cudaStream_t)stream;
-  for (int m = 1; m < n_steps; ++m) {
-    q.f[0] = states + (m - 1) * stride;
-    q.f[1] = states + m * stride;
-    if (int rc = fused_enqueue(&q, LBM_MODE_STEP, it_first + m, 1, 0, 0, m == 1, st)) return rc;
-  }
-  return LBM_OK;
+  return fused_enqueue_chain(p, it_first, n_steps, states, stride, (cudaStream_t)stream);
 }
 
 extern "C" int lbm_adjoint_sweep(const lbm_problem* p, const lbm_adjoint* adj, int64_t it_first,
@@ -777,10 +781,12 @@ extern "C" int lbm_adjoint_sweep(const lbm_problem* p, const lbm_adjoint* adj, i
   }
   double* lam[2] = {lam0, lam1};
   int cur = parity;
+  AdjArgs A;
+  adjoint_prepare(p, adj, A);
   for (int64_t n = it_first + n_steps; n > it_first; --n) {
     const double* x_prev = states + (n - 1 - it_first) * stride;
-    if (int rc = adjoint_enqueue(p, adj, n, x_prev, lam[cur], lam[cur ^ 1], (cudaStream_t)stream,
-                                 fn))
+    if (int rc = adjoint_launch(p, adj, A, n, x_prev, lam[cur], lam[cur ^ 1],
+                                (cudaStream_t)stream, fn))
       return rc;
     cur ^= 1;
   }

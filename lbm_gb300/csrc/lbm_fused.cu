@@ -263,6 +263,7 @@ FusedArgs make_args(const lbm_problem* p, int mode, unsigned flags) {
   a.advance_at = 0;
   a.check_finite = (flags & LBM_FLAG_CHECK_FINITE) && p->status_flags ? 1 : 0;
   a.bulk_tma = (flags & LBM_FLAG_BULK_REGISTERS) ? 0 : 1;
+  a.tma_stall = (flags & LBM_FLAG_TEST_STALL) ? 1 : 0;
   a.wall_macro = (flags & LBM_FLAG_WALL_MACRO) && p->rho_out && p->u_out ? 1 : 0;
   return a;
 }
@@ -307,6 +308,25 @@ template <class St>
 static int tile_cells_of(bool half) {
   using Sh = typename TmaShapeOf<St>::type;
   return half ? TmaHalf<Sh>::type::kCells : Sh::kCells;
+}
+
+int fused_enqueue_chain(const lbm_problem* p, long long it0, int n_steps, double* states,
+                        long long stride, cudaStream_t st) {
+  FusedArgs a = make_args(p, LBM_MODE_STEP, 0);
+  a.drag_hist = nullptr;
+  a.write_macro = 0;
+  for (int m = 1; m < n_steps; ++m) {
+    if (m == 1) k_set_it<<<1, 1, 0, st>>>(a.it_dev, a.step_done, it0 + 1);
+    a.fin = states + (m - 1) * stride;
+    a.fout = states + m * stride;
+    launch_store<StoreF64>(a, LBM_MODE_STEP, st, nullptr, nullptr, nullptr);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("lbm_adjoint_recompute: launch failed: %s", cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
 }
 
 int tma_tile_cells(int precision, bool half) {

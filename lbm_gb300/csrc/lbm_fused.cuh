@@ -69,6 +69,7 @@ struct alignas(16) FusedArgs {
   double* g_out;
   unsigned* status;
   int bulk_tma;  // 16-bit forms: TMA-staged bulk kernel (else register-pipelined)
+  int tma_stall;  // LBM_FLAG_TEST_STALL: the producer withholds each block's first tile
   int mode;
   int write_macro;
   int wall_macro;

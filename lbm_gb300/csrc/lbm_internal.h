@@ -15,6 +15,11 @@ int fused_enqueue(const lbm_problem* p, int mode, long long it0, int n_steps, in
                   unsigned flags, bool set_it, cudaStream_t st, cudaEvent_t* ev = nullptr);
 int fused_kernels_per_step(const lbm_problem* p, int mode);
 int fused_set_it(const lbm_problem* p, long long value, cudaStream_t st);
+// FP64 steps it0 + 1 .. it0 + n_steps - 1 along a chain of state slots:
+// step m reads states + (m - 1) * stride and writes states + m * stride (no
+// drag history).  The arguments are built once for the whole chain.
+int fused_enqueue_chain(const lbm_problem* p, long long it0, int n_steps, double* states,
+                        long long stride, cudaStream_t st);
 }  // namespace lbm
 
 #define LBM_CUDA_CHECK(call, what)                                              \

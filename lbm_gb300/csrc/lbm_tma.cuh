@@ -215,6 +215,7 @@ __device__ __forceinline__ void tma_produce(const Src& src, int n_tiles, unsigne
       break;
     }
     const FusedArgs& a = src.args(t);
+    if (a.tma_stall && k == 0) continue;  // failure-path test: tile 0 never arrives
     const S* fin = (const S*)a.fin;
     const long long Ns = a.Ns, c0 = src.first(t);
     const int sy = a.sy, len = src.count(t);
@@ -234,12 +235,13 @@ __device__ __forceinline__ void tma_produce(const Src& src, int n_tiles, unsigne
                 (unsigned)(r.hi - r.lo) * (unsigned)sizeof(S), full0 + 8 * s);
     }
   }
-  if (!ok) {
-    if (status) atomicOr(status, 8u);
-    // the copies of the last issued tiles may still be in flight
-    for (int kk = k - NST < 0 ? 0 : k - NST; kk < k; ++kk)
-      mbar_wait(full0 + 8 * (kk % NST), (kk / NST) & 1);
-  }
+  if (!ok && status) atomicOr(status, 8u);
+  // The block must not exit with copies in flight: wait (bounded) for the
+  // last tiles issued into each stage.  After a normal run the consumers
+  // have waited for them already and these waits return at once; after a
+  // consumer gave up they keep the copies from landing in a freed block.
+  for (int kk = k - NST < 0 ? 0 : k - NST; kk < k; ++kk)
+    mbar_wait(full0 + 8 * (kk % NST), (kk / NST) & 1);
 }
 
 // The kernel body; every thread of the block calls it.  status: where a

@@ -343,7 +343,10 @@ class FusedEngine:
     def step_flags(self):
         if self.bulk_kernel not in ("tma", "registers"):
             raise ValueError("bulk_kernel is 'tma' or 'registers'")
-        return _lib.FLAG_BULK_REGISTERS if self.bulk_kernel == "registers" else 0
+        flags = _lib.FLAG_BULK_REGISTERS if self.bulk_kernel == "registers" else 0
+        if getattr(self, "test_stall", False):  # failure-path test (LBM_FLAG_TEST_STALL)
+            flags |= _lib.FLAG_TEST_STALL
+        return flags
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

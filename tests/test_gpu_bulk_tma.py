@@ -49,8 +49,7 @@ CASES = {"obstacle_array_2048x512": _obstacle_array, "cavity64": lambda: _cavity
          "cavity70_padded": lambda: _cavity(70), "turek_1100x200": _turek}
 
 
-def _run(make, precision, kernel, steps):
-    import torch
+def _engine(make, precision, kernel, steps):
     import lbm_gb300
     from lbm_gb300.engine import FusedEngine, trace_bc_program
     app = make()
@@ -66,6 +65,12 @@ def _run(make, precision, kernel, steps):
     base, vec, scale = app.bc_schedule(lat)
     eng.set_bc_schedule(base, vec, scale(np.arange(steps + 8)), it0=0)
     eng.collide_from_g(0, macro=False)
+    return eng
+
+
+def _run(make, precision, kernel, steps):
+    import torch
+    eng = _engine(make, precision, kernel, steps)
     eng.steps(1, steps // 2, graph=False)
     eng.steps(1 + steps // 2, steps - steps // 2, graph=True)
     eng.check_status()
@@ -82,3 +87,23 @@ def test_tma_equals_register_kernel(cuda, case, precision):
     f_r, d_r = _run(CASES[case], precision, "registers", steps)
     assert np.array_equal(f_t, f_r)
     assert np.array_equal(d_t, d_r)
+
+
+def test_stage_wait_timeout_reports_status(cuda):
+    """The failure path of the bounded waits: with LBM_FLAG_TEST_STALL the
+    producer withholds each block's first tile, the consumers' wait on it runs
+    out (0.5 s), the kernel sets status bit 3 and returns; the host raises on
+    it, and the context keeps working (a fresh start then steps normally)."""
+    import torch
+    eng = _engine(CASES["cavity64"], "f16s", "tma", 20)
+    eng.test_stall = True
+    eng.steps(1, 1, graph=False)
+    torch.cuda.synchronize()
+    with pytest.raises(RuntimeError, match="stage wait timed out"):
+        eng.check_status()
+    eng.test_stall = False
+    eng.status.zero_()
+    eng.collide_from_g(0, macro=False)
+    eng.steps(1, 10, graph=False)
+    eng.check_status()
+    assert bool(torch.isfinite(eng.f[eng.cur].float()).all())
