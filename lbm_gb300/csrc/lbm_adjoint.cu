@@ -570,12 +570,14 @@ __device__ double adj_corner(const AdjArgs& A, int w) {
 // blocks [0, nbb) bulk cells, one per thread; blocks [nbb, nbb + nbs) special
 // cells other than corners, one per warp; the last block the corner ops,
 // one per warp.  Corner chains, special cells and bulk cells run side by
-// side.  Each block adds its part of d/d om_p to grad_omega[block].
+// side; the long special and corner chains are scheduled first (launch
+// order rotated by nbb), the bulk blocks fill in behind them.  Each block
+// adds its part of d/d om_p to grad_omega[block].
 __global__ void __launch_bounds__(128) k_adj_cells(AdjArgs A, int nbb, int nbs) {
   __shared__ double sh[128];
   const FusedArgs& a = A.f;
   double dom = 0.0;
-  const int b = blockIdx.x;
+  const int b = (int)((blockIdx.x + (unsigned)nbb) % (unsigned)(nbb + nbs + 1));
   if (b < nbb) {
     dom = adj_bulk_cell(A, (long long)b * blockDim.x + threadIdx.x);
   } else if (b < nbb + nbs) {
