@@ -337,7 +337,7 @@ def measure_sweep(steps):
     from lbm_gb300.batch import Batch, autotune, serial_loop_mlups, sweep_apps, time_batch
     t0 = time.perf_counter()
     # BC schedule length: the autotuner's trials (24 configurations x 250
-    # iterations, then 5 x (K + 200) and 4 x (K + 200), rolled back
+    # iterations, then 5 x (K + 200) and 6 x (K + 200), rolled back
     # afterwards), the timed iterations and the serial loops.
     b = Batch(sweep_apps(seed=2024), precision=SWEEP_FORM, max_steps=steps + 12000)
     setup_s = time.perf_counter() - t0

@@ -329,11 +329,14 @@ def autotune(batch, steps=60, space=None, k_space=(10, 25, 50, 100, 200),
     if stream_space:
         k = best[0]["k_steps"]
         n = k * max(1, -(-steps // k))
-        # with a TMA-staged bulk phase, both its shapes (the half-width one
-        # leaves room on each SM for the other groups' kernels)
+        # the winner, and for the 16-bit forms the TMA-staged bulk phase in
+        # both its shapes (the half-width one leaves room on each SM for the
+        # other groups' kernels; alone on the GPU it may lose to the winner)
         bases = [dict(best[0])]
-        if best[0].get("bulk_tma"):
-            bases.append(dict(best[0], bulk_tma=3 - best[0]["bulk_tma"]))
+        if batch.precision in TMA_FORMS:
+            for tma in (1, 2):
+                if best[0].get("bulk_tma", 0) != tma:
+                    bases.append(dict(best[0], bulk_tma=tma))
         for g, base in itertools.product(stream_space, bases):
             cfg = dict(base, streams=g)
             batch.set_config(cfg)
