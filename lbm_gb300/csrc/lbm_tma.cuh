@@ -13,10 +13,11 @@
 // vectors and six halo cells from the stage, arrives on the stage's `empty`
 // mbarrier (batched tiles: after the update, see BatchTiles), and runs
 // bulk_group_vec_update (the update of the register-pipelined kernel, so
-// both give the same bits).  Every wait is
-// bounded (kWaitNs): a wait that runs out sets status bit 3 and the thread
-// leaves its loop; the producer then waits (bounded) for its copies still in
-// flight before the block exits.
+// both give the same bits).  Every wait is bounded (kWaitNs): a wait that
+// runs out sets status bit 3 and the thread leaves its loop.  Before the
+// block exits, the producer waits (bounded) for the last copies it issued,
+// so that none lands in a freed block (LBM_FLAG_TEST_STALL exercises that
+// path).
 //
 // Alignment: lattice rows are padded to a multiple of 8 elements (16 bytes),
 // so c0, len, sy and the plane size are multiples of 8 elements; every copy
