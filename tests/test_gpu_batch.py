@@ -84,3 +84,27 @@ def test_sweep_generator_is_seeded_and_in_range():
         assert 64 <= x.ny <= 256 and x.nx == 4 * x.ny and 1 <= len(x.obstacles) <= 6
         assert 100.0 <= x.Re_lbm <= 2000.0
         assert x.tau_lbm >= 0.53 - 1e-12
+
+
+def test_autotune_puts_the_lattices_back(cuda):
+    """The autotuner's trials advance the lattices; afterwards every lattice
+    holds the state it had before them, and the batch continues from the
+    same iteration (a tiny candidate space keeps this short)."""
+    import torch
+    from lbm_gb300.batch import autotune
+    b = Batch(_apps(), precision="f16sr")
+    b.advance(20, k=10)
+    torch.cuda.synchronize()
+    before = [e.f[e.cur].clone() for e in b.engines]
+    it0, parity0 = b.it, b.parity
+    space = {"persistent": [0], "tile_rounds": [1], "vec_bytes": [16], "bulk_threads": [64],
+             "k_steps": [10]}
+    best, trials = autotune(b, steps=20, space=space, k_space=(10,), stream_space=(2,))
+    assert b.it == it0 and b.parity == parity0
+    for e, f in zip(b.engines, before):
+        assert e.cur == parity0
+        assert torch.equal(e.f[e.cur], f)
+    assert len(trials) >= 3 and best["k_steps"] == 10
+    b.advance(10, k=10)
+    b.check()
+    b.close()
