@@ -31,7 +31,7 @@ struct lbm_batch {
   lbm::FusedArgs* d_args;   // [2][n_cases]
   int4* d_bulk_tiles;       // (case, first, count, vectorised); TMA: (case, first cell, cells, 2)
   int n_bulk_tiles;
-  int4* d_special_tiles;    // (case, first, count, 0)
+  int4* d_special_tiles;    // (case, first, count, links in the tile)
   int n_special_tiles;
   int2* d_drag_items;       // (case, obstacle)
   int n_drag_items;
@@ -382,11 +382,28 @@ extern "C" int lbm_batch_create(lbm_batch** out, const lbm_problem* cases, int32
       for (long long x = 0; x < N; x += cfg->scalar_tile_cells)
         bulk.push_back(make_int4(c, (int)x, (int)std::min<long long>(cfg->scalar_tile_cells, N - x), 0));
     }
-    for (int s = 0; s < p.n_special; s += 128)
-      special.push_back(make_int4(c, s, std::min(128, p.n_special - s), 0));
+    // special tiles carry their number of links (w), the longest chains
+    std::vector<int> link_start((size_t)p.n_special + 1, 0);
+    if (p.n_links > 0 &&
+        cudaMemcpy(link_start.data(), p.special_link_start, link_start.size() * sizeof(int),
+                   cudaMemcpyDeviceToHost) != cudaSuccess)
+      std::fill(link_start.begin(), link_start.end(), 0);
+    for (int s = 0; s < p.n_special; s += 128) {
+      const int n = std::min(128, p.n_special - s);
+      special.push_back(make_int4(c, s, n, link_start[s + n] - link_start[s]));
+    }
     if (p.drag_hist && p.n_links > 0)
       for (int o = 0; o < p.n_obstacles; ++o) drag.push_back(make_int2(c, o));
   }
+  // Special tiles with the most links first (stable): their chains are the
+  // longest, so they start in the first wave and the short wall tiles fill
+  // in behind them.
+#ifndef LBM_SPECIAL_TILE_ORDER
+#define LBM_SPECIAL_TILE_ORDER 1
+#endif
+  if (LBM_SPECIAL_TILE_ORDER)
+    std::stable_sort(special.begin(), special.end(),
+                     [](const int4& x, const int4& y) { return x.w > y.w; });
   // The persistent bulk kernel's tile queue (queue[0]) is reset for the next
   // iteration by the special-cell kernel, so that schedule needs special
   // tiles.  Every lattice has them today (problem_check asks for at least the
