@@ -6,7 +6,9 @@
 // (pull), applies set_bc(it-1) and the drag/lift of it-1, and takes macro,
 // equilibrium and collision of g(it) to write g_up(it).  Two kernels do this:
 //
-//   k_bulk    every cell not on a wall: pull 9 values, collide, write 9.
+//   k_bulk    every cell not on a wall: pull 9 values, collide, write 9
+//             (k_bulk_q60 for the plain form, the TMA-staged k_bulk_tma or
+//             the register-pipelined k_bulk_vec for the 16-bit forms).
 //   k_special every wall cell and every cell owning an obstacle link (a short
 //             sorted list): pull, links (IBB/BB), Zou-He walls in the app's
 //             order, corners, per-link drag terms, collide.  It overwrites
@@ -107,10 +109,11 @@ static void launch_mode(const FusedArgs& a0, cudaStream_t st, cudaEvent_t* ev, D
   const bool side = lane && with_drag && with_special && MODE == LBM_MODE_STEP && !ev;
   const int tb = 256;
   const long long nb = (a.Ns + tb - 1) / tb;
-  // 16-byte vectors (8 cells per thread) for the 16-bit storage forms; FP32
-  // takes the one-cell-per-thread kernel, measured faster on 8192x2048
-  // (176 vs 190 us per bulk launch with 4-cell vectors), while 8-cell
-  // vectors beat 4-cell ones for the 16-bit forms (103-112 vs 108-118 us).
+  // 16-bit storage forms: the TMA-staged kernel, or with
+  // LBM_FLAG_BULK_REGISTERS the register-pipelined one with 16-byte vectors
+  // (8 cells per thread; 4-cell vectors: 108-118 vs 103-112 us).  FP32 takes
+  // the one-cell-per-thread kernel, measured faster on 8192x2048 (176 vs
+  // 190 us per bulk launch with 4-cell vectors).
   constexpr int kVec = 16 / (int)sizeof(typename St::S);
   constexpr bool kUseVec = MODE == LBM_MODE_STEP && St::kShift && sizeof(typename St::S) == 2;
   a.advance_at = with_drag && !side ? 2 : (with_special ? 1 : 0);
