@@ -4,7 +4,9 @@
 // collision: the state kept in HBM is the post-collision population g_up of
 // the previous iteration.  Iteration `it` then reads g_up(it-1), streams it
 // (pull), applies set_bc(it-1) and the drag/lift of it-1, and takes macro,
-// equilibrium and collision of g(it) to write g_up(it).  Two kernels do this:
+// equilibrium and collision of g(it) to write g_up(it).  Three kernels do
+// this (in enqueues of several steps the drag kernel of step k runs on a
+// second stream beside the bulk kernel of step k + 1):
 //
 //   k_bulk    every cell not on a wall: pull 9 values, collide, write 9
 //             (k_bulk_q60 for the plain form, the TMA-staged k_bulk_tma or
